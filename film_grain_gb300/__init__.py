@@ -1,0 +1,410 @@
+"""film_grain_gb300 -- GB300 (sm_103a) Monte Carlo film-grain integrators.
+
+A drop-in for the hot path of joseph-wardle/film_grain: the pixel-wise and grain-wise integrators
+(src/pixelwise.rs, src/grainwise.rs), their RNG streams (src/rng.rs) and the host arithmetic of the
+crate's render entry points (src/params.rs, src/model.rs, src/choose.rs, src/color.rs, src/lib.rs).
+Every call goes through the C-ABI of ``libfg_gb300.so`` (include/film_grain_gb300.h); this module
+mirrors the crate's names, argument meanings and errors:
+
+    params = ParamsBuilder(radius_mean=0.12, n_samples=64, seed=42).build()
+    derived = derive_common(params, (width, height))
+    lam = lambda_plane(normalize_plane(plane)[0], derived.inv_e_pi_r2)
+    out = render_pixelwise(lam, params, derived)            # numpy in -> numpy out
+    out = render_grainwise(lam_cuda_tensor, params, derived)  # torch CUDA tensor in -> tensor out
+    image, stats = render_with_input_image(rgb_f32, params)   # whole image, u8 RGB out
+
+There is no CPU fallback: without the native library (or without a GPU for the render calls) the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import os
+from dataclasses import dataclass, field
+from typing import Callable, Optional, Tuple
+
+import numpy as np
+
+__all__ = [
+    "RadiusDist", "Algo", "ColorMode", "MaxRadius", "Roi", "ParamsBuilder", "Params", "Derived", "RenderStats",
+    "RenderError", "ParamsError", "CancelledError", "GpuError", "derive_common", "default_cell_delta",
+    "normalize_plane", "lambda_plane", "choose_algorithm", "render_pixelwise", "render_grainwise",
+    "render_with_input_image", "dry_run_with_input_image", "lib", "pixelwise_diagnostics", "make_offsets",
+]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libfg_gb300.so")
+
+
+class RadiusDist(enum.IntEnum):
+    Const = 0
+    Lognorm = 1
+
+
+class Algo(enum.IntEnum):
+    Auto = 0
+    Grain = 1
+    Pixel = 2
+
+
+class ColorMode(enum.IntEnum):
+    Luma = 0
+    Rgb = 1
+
+
+@dataclass(frozen=True)
+class MaxRadius:
+    """MaxRadius::Absolute(v) / MaxRadius::Quantile(p) (src/params.rs:38-42)."""
+    kind: str
+    value: float
+
+    @staticmethod
+    def Absolute(v: float) -> "MaxRadius":
+        return MaxRadius("absolute", float(v))
+
+    @staticmethod
+    def Quantile(p: float) -> "MaxRadius":
+        return MaxRadius("quantile", float(p))
+
+
+@dataclass(frozen=True)
+class Roi:
+    x0: int
+    y0: int
+    x1: int
+    y1: int
+
+
+# ------------------------------------------------------------------ errors (RenderError, src/lib.rs:28-44)
+class RenderError(RuntimeError):
+    """Base of the render errors; ``code`` is the C-ABI fg_status."""
+
+    def __init__(self, msg: str, code: int):
+        super().__init__(msg)
+        self.code = code
+
+
+class ParamsError(RenderError, ValueError):
+    pass
+
+
+class CancelledError(RenderError):
+    pass
+
+
+class GpuError(RenderError):
+    pass
+
+
+_FG_OK, _FG_PARAMS, _FG_CANCELLED, _FG_CUDA, _FG_INVALID, _FG_UNSUPPORTED, _FG_NOMEM, _FG_INTERNAL = range(8)
+
+
+# ------------------------------------------------------------------ C structs
+class _BuilderC(ctypes.Structure):
+    _fields_ = [("radius_dist", ctypes.c_int32), ("radius_mean", ctypes.c_float), ("radius_stddev", ctypes.c_float),
+                ("zoom", ctypes.c_float), ("sigma_px", ctypes.c_float), ("n_samples", ctypes.c_uint32),
+                ("algo", ctypes.c_int32), ("max_radius_kind", ctypes.c_int32), ("max_radius_value", ctypes.c_float),
+                ("cell_delta", ctypes.c_float), ("color_mode", ctypes.c_int32), ("has_roi", ctypes.c_int32),
+                ("roi_x0", ctypes.c_uint32), ("roi_y0", ctypes.c_uint32), ("roi_x1", ctypes.c_uint32),
+                ("roi_y1", ctypes.c_uint32), ("size_w", ctypes.c_uint32), ("size_h", ctypes.c_uint32),
+                ("seed", ctypes.c_uint64)]
+
+
+class _ParamsC(ctypes.Structure):
+    _fields_ = [("radius_dist", ctypes.c_int32), ("radius_mean", ctypes.c_float), ("radius_stddev", ctypes.c_float),
+                ("radius_log_mu", ctypes.c_float), ("radius_log_sigma", ctypes.c_float),
+                ("has_log_params", ctypes.c_int32), ("zoom", ctypes.c_float), ("sigma_px", ctypes.c_float),
+                ("n_samples", ctypes.c_uint32), ("algo", ctypes.c_int32), ("max_radius_kind", ctypes.c_int32),
+                ("max_radius_value", ctypes.c_float), ("cell_delta", ctypes.c_float), ("color_mode", ctypes.c_int32),
+                ("has_roi", ctypes.c_int32), ("roi_x0", ctypes.c_uint32), ("roi_y0", ctypes.c_uint32),
+                ("roi_x1", ctypes.c_uint32), ("roi_y1", ctypes.c_uint32), ("size_w", ctypes.c_uint32),
+                ("size_h", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+
+
+class _DerivedC(ctypes.Structure):
+    _fields_ = [("input_width", ctypes.c_int64), ("input_height", ctypes.c_int64), ("output_width", ctypes.c_int64),
+                ("output_height", ctypes.c_int64), ("inv_e_pi_r2", ctypes.c_float), ("rm", ctypes.c_float),
+                ("delta", ctypes.c_float), ("n_offsets", ctypes.c_uint32)]
+
+
+class _StatsC(ctypes.Structure):
+    _fields_ = [("algorithm", ctypes.c_int32), ("input_width", ctypes.c_int64), ("input_height", ctypes.c_int64),
+                ("output_width", ctypes.c_int64), ("output_height", ctypes.c_int64), ("n_samples", ctypes.c_uint32),
+                ("sigma_ratio", ctypes.c_float), ("rm_ratio", ctypes.c_float)]
+
+
+# Every symbol include/film_grain_gb300.h declares, with its ctypes signature.
+_P = ctypes.POINTER
+_f32p = _P(ctypes.c_float)
+_vp = ctypes.c_void_p
+SIGNATURES = {
+    "fg_params_build": (ctypes.c_int, [_P(_BuilderC), _P(_ParamsC)]),
+    "fg_derive": (ctypes.c_int, [_P(_ParamsC), ctypes.c_int64, ctypes.c_int64, _P(_DerivedC), _vp, _vp]),
+    "fg_choose_algorithm": (ctypes.c_int32, [_P(_ParamsC), _P(_DerivedC)]),
+    "fg_default_cell_delta": (ctypes.c_float, [ctypes.c_float]),
+    "fg_normalize_plane": (ctypes.c_float, [_vp, ctypes.c_int64, _vp]),
+    "fg_lambda_plane": (None, [_vp, ctypes.c_int64, ctypes.c_float, _vp]),
+    "fg_render_pixelwise": (ctypes.c_int, [_vp, _P(_ParamsC), _P(_DerivedC), _vp, _vp, _vp, _vp]),
+    "fg_render_grainwise": (ctypes.c_int, [_vp, _P(_ParamsC), _P(_DerivedC), _vp, _vp, _vp, _vp]),
+    "fg_render_pixelwise_async": (ctypes.c_int, [_vp, _P(_ParamsC), _P(_DerivedC), _vp, _vp, _vp]),
+    "fg_render_grainwise_async": (ctypes.c_int, [_vp, _P(_ParamsC), _P(_DerivedC), _vp, _vp, _vp]),
+    "fg_render_image": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, _P(_ParamsC), _vp, _P(_StatsC), _vp,
+                                       _vp]),
+    "fg_dry_run": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, _P(_ParamsC), _P(_StatsC)]),
+    "fg_last_error_message": (ctypes.c_char_p, []),
+    "fg_version": (ctypes.c_char_p, []),
+    "fg_pixelwise_diagnostics": (None, [_P(ctypes.c_ulonglong)]),
+}
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def lib() -> ctypes.CDLL:
+    """The native library; raises if it has not been built (there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"film_grain_gb300 native library missing: {LIB_PATH} "
+                              "(build it with film_grain_gb300.build.build())")
+        handle = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = handle
+    return _lib
+
+
+def _raise(code: int):
+    if code == _FG_OK:
+        return
+    msg = (lib().fg_last_error_message() or b"").decode()
+    if code == _FG_PARAMS:
+        raise ParamsError(msg, code)
+    if code == _FG_CANCELLED:
+        raise CancelledError(msg or "cancelled", code)
+    if code in (_FG_CUDA, _FG_NOMEM, _FG_INTERNAL):
+        raise GpuError(msg, code)
+    raise RenderError(msg, code)
+
+
+# ------------------------------------------------------------------ params
+@dataclass
+class ParamsBuilder:
+    """ParamsBuilder (src/params.rs:70-91); defaults are the CLI's (src/main.rs:94-247)."""
+    radius_mean: float = 0.10
+    radius_dist: RadiusDist = RadiusDist.Const
+    radius_stddev: float = 0.0
+    zoom: float = 1.0
+    sigma_px: float = 0.8
+    n_samples: int = 32
+    algo: Algo = Algo.Auto
+    max_radius: MaxRadius = field(default_factory=lambda: MaxRadius.Quantile(0.999))
+    cell_delta: Optional[float] = None
+    color_mode: ColorMode = ColorMode.Luma
+    roi: Optional[Roi] = None
+    size: Optional[Tuple[int, Optional[int]]] = None
+    seed: int = 5489
+
+    def build(self) -> "Params":
+        b = _BuilderC()
+        b.radius_dist = int(self.radius_dist)
+        b.radius_mean = self.radius_mean
+        b.radius_stddev = self.radius_stddev
+        b.zoom = self.zoom
+        b.sigma_px = self.sigma_px
+        b.n_samples = max(0, int(self.n_samples))
+        b.algo = int(self.algo)
+        b.max_radius_kind = 0 if self.max_radius.kind == "absolute" else 1
+        b.max_radius_value = self.max_radius.value
+        b.cell_delta = float("nan") if self.cell_delta is None else float(self.cell_delta)
+        b.color_mode = int(self.color_mode)
+        if self.roi is not None:
+            b.has_roi = 1
+            b.roi_x0, b.roi_y0, b.roi_x1, b.roi_y1 = self.roi.x0, self.roi.y0, self.roi.x1, self.roi.y1
+        if self.size is not None:
+            w, h = self.size
+            if w == 0:
+                raise ParamsError("parameter error: size: output width must be > 0", _FG_PARAMS)
+            if h is not None and h == 0:
+                raise ParamsError("parameter error: size: output height must be > 0", _FG_PARAMS)
+            b.size_w, b.size_h = int(w), int(h or 0)
+        b.seed = int(self.seed) & 0xFFFFFFFFFFFFFFFF
+        out = _ParamsC()
+        _raise(lib().fg_params_build(ctypes.byref(b), ctypes.byref(out)))
+        return Params(out)
+
+
+class Params:
+    """Resolved Params (src/params.rs:45-68) backed by the C struct."""
+
+    def __init__(self, c: _ParamsC):
+        self._c = c
+
+    def __getattr__(self, name):
+        return getattr(self._c, name)
+
+    @property
+    def c(self) -> _ParamsC:
+        return self._c
+
+    def __repr__(self):
+        fields = ", ".join(f"{n}={getattr(self._c, n)!r}" for n, _ in _ParamsC._fields_)
+        return f"Params({fields})"
+
+
+@dataclass
+class Derived:
+    """Derived (src/model.rs:167-179)."""
+    input_width: int
+    input_height: int
+    output_width: int
+    output_height: int
+    inv_e_pi_r2: float
+    rm: float
+    delta: float
+    offsets: np.ndarray
+    offsets_input: np.ndarray
+    _c: _DerivedC = field(repr=False, default=None)
+
+
+@dataclass
+class RenderStats:
+    """RenderStats (src/lib.rs:46-55)."""
+    algorithm: Algo
+    input_size: Tuple[int, int]
+    output_size: Tuple[int, int]
+    n_samples: int
+    sigma_ratio: float
+    rm_ratio: float
+
+
+def _stats(s: _StatsC) -> RenderStats:
+    return RenderStats(Algo(s.algorithm), (s.input_width, s.input_height), (s.output_width, s.output_height),
+                       s.n_samples, s.sigma_ratio, s.rm_ratio)
+
+
+def default_cell_delta(radius_mean: float) -> float:
+    return lib().fg_default_cell_delta(radius_mean)
+
+
+def derive_common(params: Params, input_size: Tuple[int, int]) -> Derived:
+    """derive_common (src/model.rs:181-226), including make_offsets (src/rng.rs:9-24)."""
+    w, h = input_size
+    n = params.n_samples
+    offs = np.zeros((n, 2), np.float32)
+    offs_in = np.zeros((n, 2), np.float32)
+    d = _DerivedC()
+    _raise(lib().fg_derive(ctypes.byref(params.c), int(w), int(h), ctypes.byref(d), offs.ctypes.data,
+                           offs_in.ctypes.data))
+    return Derived(d.input_width, d.input_height, d.output_width, d.output_height, d.inv_e_pi_r2, d.rm, d.delta,
+                   offs, offs_in, d)
+
+
+def make_offsets(params: Params) -> np.ndarray:
+    return derive_common(params, (1, 1)).offsets
+
+
+def normalize_plane(plane: np.ndarray) -> Tuple[np.ndarray, float]:
+    src = np.ascontiguousarray(plane, np.float32)
+    dst = np.empty_like(src)
+    mx = lib().fg_normalize_plane(src.ctypes.data, src.size, dst.ctypes.data)
+    return dst, mx
+
+
+def lambda_plane(normalized: np.ndarray, inv_e_pi_r2: float) -> np.ndarray:
+    src = np.ascontiguousarray(normalized, np.float32)
+    dst = np.empty_like(src)
+    lib().fg_lambda_plane(src.ctypes.data, src.size, inv_e_pi_r2, dst.ctypes.data)
+    return dst
+
+
+def choose_algorithm(params: Params, derived: Derived) -> Algo:
+    return Algo(lib().fg_choose_algorithm(ctypes.byref(params.c), ctypes.byref(derived._c)))
+
+
+# ------------------------------------------------------------------ integrators
+def _is_torch_cuda(x) -> bool:
+    return type(x).__module__.startswith("torch") and getattr(x, "is_cuda", False)
+
+
+class _Cancel:
+    """A cancel flag the library polls between launches (Fn() -> bool in the crate)."""
+
+    def __init__(self, cancel: Optional[Callable[[], bool]]):
+        self.flag = ctypes.c_int32(1 if (cancel is not None and cancel()) else 0)
+
+    @property
+    def ptr(self):
+        return ctypes.addressof(self.flag)
+
+
+def _render(fn_name: str, lam, params: Params, derived: Derived, cancel, offs: np.ndarray):
+    h, w = derived.input_height, derived.input_width
+    oh, ow = derived.output_height, derived.output_width
+    cflag = _Cancel(cancel)
+    fn = getattr(lib(), fn_name)
+    if _is_torch_cuda(lam):
+        import torch
+        if lam.dtype != torch.float32 or not lam.is_contiguous() or lam.numel() != w * h:
+            raise RenderError("lambda must be a contiguous float32 tensor of input_width*input_height", _FG_INVALID)
+        out = torch.empty((oh, ow), dtype=torch.float32, device=lam.device)
+        stream = torch.cuda.current_stream(lam.device).cuda_stream
+        _raise(fn(lam.data_ptr(), ctypes.byref(params.c), ctypes.byref(derived._c), offs.ctypes.data,
+                  out.data_ptr(), cflag.ptr, stream))
+        return out
+    src = np.ascontiguousarray(lam, np.float32)
+    if src.size != w * h:
+        raise RenderError("lambda plane size does not match the derived input size", _FG_INVALID)
+    out = np.empty((oh, ow), np.float32)
+    _raise(fn(src.ctypes.data, ctypes.byref(params.c), ctypes.byref(derived._c), offs.ctypes.data, out.ctypes.data,
+              cflag.ptr, None))
+    return out
+
+
+def render_pixelwise(lam, params: Params, derived: Derived, cancel: Optional[Callable[[], bool]] = None):
+    """render_pixelwise (src/pixelwise.rs:11-45).  lam: numpy (host) or torch CUDA tensor."""
+    return _render("fg_render_pixelwise", lam, params, derived, cancel,
+                   np.ascontiguousarray(derived.offsets_input, np.float32))
+
+
+def render_grainwise(lam, params: Params, derived: Derived, cancel: Optional[Callable[[], bool]] = None):
+    """render_grainwise (src/grainwise.rs:12-124).  lam: numpy (host) or torch CUDA tensor."""
+    return _render("fg_render_grainwise", lam, params, derived, cancel,
+                   np.ascontiguousarray(derived.offsets, np.float32))
+
+
+def pixelwise_diagnostics() -> Tuple[int, int, int, int]:
+    """(slow-path samples, unstaged blocks, subdivisions, blocks) of this thread's last pixel-wise render."""
+    arr = (ctypes.c_ulonglong * 4)()
+    lib().fg_pixelwise_diagnostics(arr)
+    return tuple(int(v) for v in arr)
+
+
+def _output_size(rgb_shape, params: Params) -> Tuple[int, int]:
+    h, w = rgb_shape[0], rgb_shape[1]
+    st = _StatsC()
+    _raise(lib().fg_dry_run(w, h, ctypes.byref(params.c), ctypes.byref(st)))
+    return st.output_width, st.output_height
+
+
+def render_with_input_image(rgb: np.ndarray, params: Params, cancel: Optional[Callable[[], bool]] = None):
+    """render_with_input_image[_cancelable] (src/lib.rs:78-93): f32 RGB (H, W, 3) -> (u8 RGB, RenderStats)."""
+    src = np.ascontiguousarray(rgb, np.float32)
+    if src.ndim != 3 or src.shape[2] != 3:
+        raise RenderError("expected an (H, W, 3) RGB array", _FG_INVALID)
+    ow, oh = _output_size(src.shape, params)
+    out = np.empty((oh, ow, 3), np.uint8)
+    st = _StatsC()
+    cflag = _Cancel(cancel)
+    _raise(lib().fg_render_image(src.ctypes.data, src.shape[1], src.shape[0], ctypes.byref(params.c),
+                                 out.ctypes.data, ctypes.byref(st), cflag.ptr, None))
+    return out, _stats(st)
+
+
+def dry_run_with_input_image(rgb_shape, params: Params) -> RenderStats:
+    """dry_run_with_input_image (src/lib.rs:100-104) from the input's (H, W[, 3]) shape."""
+    st = _StatsC()
+    _raise(lib().fg_dry_run(rgb_shape[1], rgb_shape[0], ctypes.byref(params.c), ctypes.byref(st)))
+    return _stats(st)

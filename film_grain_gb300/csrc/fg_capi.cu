@@ -1,0 +1,420 @@
+// fg_capi.cu -- the render entry points of the C-ABI: buffer staging, launch planning and the
+// whole-image orchestration of render_from_workspace_impl (src/lib.rs:134-173).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/film_grain_gb300.h"
+#include "fg_host.h"
+#include "fg_kernels.cuh"
+#include "fg_internal.h"
+
+namespace fg {
+
+static thread_local unsigned long long g_pw_diag[4] = {0, 0, 0, 0};
+
+fg_status cuda_error(cudaError_t e, const char *what) {
+    return set_error(e == cudaErrorMemoryAllocation ? FG_ERR_NOMEM : FG_ERR_CUDA,
+                     std::string("gpu error: ") + what + ": " + cudaGetErrorString(e));
+}
+
+#define FG_CUDA(call, what)                                  \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_error(e_, what);  \
+    } while (0)
+
+bool is_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+static bool cancelled(const volatile int32_t *cancel) { return cancel && *cancel != 0; }
+
+void offset_extents(const float *offs, uint32_t n, float ext[4]) {
+    ext[0] = ext[1] = ext[2] = ext[3] = 0.0f;
+    for (uint32_t k = 0; k < n; k++) {
+        ext[0] = std::fmin(ext[0], offs[2 * k]);
+        ext[1] = std::fmax(ext[1], offs[2 * k]);
+        ext[2] = std::fmin(ext[2], offs[2 * k + 1]);
+        ext[3] = std::fmax(ext[3], offs[2 * k + 1]);
+    }
+}
+
+static fg_status check_common(const fg_params *p, const fg_derived *d) {
+    if (!p || !d) return set_error(FG_ERR_INVALID, "null params or derived");
+    if (d->input_width <= 0 || d->input_height <= 0 || d->output_width <= 0 || d->output_height <= 0)
+        return set_error(FG_ERR_INVALID, "plane dimensions must be positive");
+    if (d->input_width > (1 << 24) || d->input_height > (1 << 24) || d->output_width > (1 << 24) ||
+        d->output_height > (1 << 24) || d->input_width * d->input_height >= (1ll << 31) ||
+        d->output_width * d->output_height >= (1ll << 31))
+        return set_error(FG_ERR_UNSUPPORTED, "plane larger than 2^31 pixels or 2^24 per side");
+    if (p->n_samples == 0 || p->n_samples > 65536) return set_error(FG_ERR_UNSUPPORTED, "n_samples must be in 1..65536");
+    if (!(p->zoom > 0.0f) || !(d->delta > 0.0f)) return set_error(FG_ERR_INVALID, "zoom and delta must be positive");
+    if (p->radius_dist == FG_RADIUS_LOGNORM && !p->has_log_params)
+        return set_error(FG_ERR_INVALID, "missing log-normal parameters");
+    return FG_OK;
+}
+
+// Pixel-wise launch plan: the largest power-of-two block edge whose staged window fits.
+PwPlan plan_pixelwise(const fg_params &p, const fg_derived &d, const float *h_offs_in) {
+    PwPlan pl;
+    offset_extents(h_offs_in, p.n_samples, pl.ext);
+    const float rm = d.rm, delta = d.delta;
+    int b;
+    for (b = 4; b > -8; b--) {
+        float B = std::ldexp(1.0f, b);
+        double wc = std::floor((B + 2.0 * rm) / delta) + 4.0;
+        if (wc <= kPwEdgeMax && wc * wc <= kPwCellMax) break;
+    }
+    pl.bsize = std::ldexp(1.0f, b);
+    const float inv_zoom = 1.0f / p.zoom;
+    float xmin = 0.5f * inv_zoom - pl.ext[1], ymin = 0.5f * inv_zoom - pl.ext[3];
+    float xmax = ((float)(d.output_width - 1) + 0.5f) * inv_zoom - pl.ext[0];
+    float ymax = ((float)(d.output_height - 1) + 0.5f) * inv_zoom - pl.ext[2];
+    pl.bx0 = (int)std::floor(xmin / pl.bsize) - 1;
+    pl.by0 = (int)std::floor(ymin / pl.bsize) - 1;
+    pl.nbx = (int)std::floor(xmax / pl.bsize) + 1 - pl.bx0 + 1;
+    pl.nby = (int)std::floor(ymax / pl.bsize) + 1 - pl.by0 + 1;
+    return pl;
+}
+
+fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_derived &d, const float *h_offs_in,
+                            const float *d_offs_in, float *d_out, CellParam *d_cells, unsigned long long *d_diag,
+                            const EpilogueArgs *colour, cudaStream_t s) {
+    const int in_w = (int)d.input_width, in_h = (int)d.input_height;
+    const int out_w = (int)d.output_width, out_h = (int)d.output_height;
+    PwPlan pl = plan_pixelwise(p, d, h_offs_in);
+    FG_CUDA(launch_cell_params(d_lam, in_w, in_h, d.delta, d_cells, s), "cell params");
+    FG_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * (size_t)out_w * out_h, s), "memset");
+    PixelwiseArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.lam = d_lam;
+    a.cells = d_cells;
+    a.offs = reinterpret_cast<const float2 *>(d_offs_in);
+    a.out = d_out;
+    a.diag = d_diag;
+    a.in_w = in_w; a.in_h = in_h; a.out_w = out_w; a.out_h = out_h;
+    a.n = (int)p.n_samples;
+    a.rm = d.rm;
+    a.delta = d.delta;
+    a.inv_zoom = 1.0f / p.zoom;
+    a.zoom = p.zoom;
+    a.bsize = pl.bsize;
+    a.inv_bsize = 1.0f / pl.bsize;
+    a.bx0 = pl.bx0; a.by0 = pl.by0; a.nbx = pl.nbx;
+    a.offx_min = pl.ext[0]; a.offx_max = pl.ext[1]; a.offy_min = pl.ext[2]; a.offy_max = pl.ext[3];
+    a.seed = p.seed;
+    a.lognorm = p.radius_dist == FG_RADIUS_LOGNORM;
+    a.radius_mean = p.radius_mean;
+    a.log_mu = (double)p.radius_log_mu;
+    a.log_sigma = (double)p.radius_log_sigma;
+    FG_CUDA(launch_pixelwise(a, pl.nby, pixelwise_smem_bytes(), s), "pixelwise kernel");
+    EpilogueArgs e;
+    if (colour) e = *colour;
+    else std::memset(&e, 0, sizeof e);
+    e.plane = d_out;
+    e.out_w = out_w; e.out_h = out_h; e.in_w = in_w; e.in_h = in_h;
+    e.inv_samples = 1.0f / (float)p.n_samples;
+    FG_CUDA(launch_epilogue(e, s), "pixelwise epilogue");
+    return FG_OK;
+}
+
+GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const float *h_offs, const float *d_lam,
+                             const float *d_offs, float *d_out) {
+    GrainwiseArgs a;
+    std::memset(&a, 0, sizeof a);
+    float ext[4];
+    offset_extents(h_offs, p.n_samples, ext);
+    a.lam = d_lam;
+    a.offs = reinterpret_cast<const float2 *>(d_offs);
+    a.out = d_out;
+    a.in_w = (int)d.input_width; a.in_h = (int)d.input_height;
+    a.out_w = (int)d.output_width; a.out_h = (int)d.output_height;
+    a.n = (int)p.n_samples;
+    a.words = (a.n + 31) / 32;
+    int pix = std::max(1, 16384 / a.words);
+    int tw = 64;
+    while (tw > 1 && tw * tw > pix) tw >>= 1;
+    a.tile_w = tw;
+    a.tile_h = std::max(1, std::min(64, pix / tw));
+    a.rm = d.rm;
+    a.zoom = p.zoom;
+    a.offx_min = ext[0]; a.offx_max = ext[1]; a.offy_min = ext[2]; a.offy_max = ext[3];
+    a.seed = p.seed;
+    a.lognorm = p.radius_dist == FG_RADIUS_LOGNORM;
+    a.radius_mean = p.radius_mean;
+    a.log_mu = (double)p.radius_log_mu;
+    a.log_sigma = (double)p.radius_log_sigma;
+    return a;
+}
+
+fg_status enqueue_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
+    if ((size_t)a.n * sizeof(float2) + (size_t)a.tile_w * a.tile_h * a.words * 4 > 200 * 1024)
+        return set_error(FG_ERR_UNSUPPORTED, "n_samples too large for the grain-wise tile");
+    FG_CUDA(launch_grainwise(a, s), "grainwise kernel");
+    return FG_OK;
+}
+
+// Stream-ordered device buffer that frees itself.
+struct DevBuf {
+    void *p = nullptr;
+    cudaStream_t s = nullptr;
+    cudaError_t alloc(size_t bytes, cudaStream_t st) {
+        s = st;
+        return cudaMallocAsync(&p, bytes ? bytes : 16, st);
+    }
+    ~DevBuf() {
+        if (p) cudaFreeAsync(p, s);
+    }
+};
+
+static void keep_pool_memory() {
+    static bool done = false;
+    if (done) return;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    done = true;
+}
+
+// Shared body of the synchronous integrator entry points.
+static fg_status render_plane_sync(int algo, const float *lambda, const fg_params *params, const fg_derived *derived,
+                                   const float *offsets, float *out, const volatile int32_t *cancel, void *stream) {
+    fg_status st = check_common(params, derived);
+    if (st != FG_OK) return st;
+    if (!lambda || !offsets || !out) return set_error(FG_ERR_INVALID, "null buffer");
+    if (cancelled(cancel)) return set_error(FG_ERR_CANCELLED, "cancelled");
+    keep_pool_memory();
+    cudaStream_t s = (cudaStream_t)stream;
+    const fg_params &p = *params;
+    const fg_derived &d = *derived;
+    const size_t n_in = (size_t)d.input_width * d.input_height, n_out = (size_t)d.output_width * d.output_height;
+    const size_t off_bytes = sizeof(float) * 2 * p.n_samples;
+
+    std::vector<float> h_offs(2 * (size_t)p.n_samples);
+    const bool offs_dev = is_device_ptr(offsets);
+    if (offs_dev) FG_CUDA(cudaMemcpy(h_offs.data(), offsets, off_bytes, cudaMemcpyDeviceToHost), "offsets D2H");
+    else std::memcpy(h_offs.data(), offsets, off_bytes);
+
+    DevBuf b_lam, b_out, b_offs, b_cells, b_diag;
+    const float *d_lam = lambda;
+    float *d_out = out;
+    const float *d_offs = offsets;
+    if (!is_device_ptr(lambda)) {
+        FG_CUDA(b_lam.alloc(sizeof(float) * n_in, s), "alloc lambda");
+        FG_CUDA(cudaMemcpyAsync(b_lam.p, lambda, sizeof(float) * n_in, cudaMemcpyHostToDevice, s), "lambda H2D");
+        d_lam = (const float *)b_lam.p;
+    }
+    const bool out_dev = is_device_ptr(out);
+    if (!out_dev) {
+        FG_CUDA(b_out.alloc(sizeof(float) * n_out, s), "alloc out");
+        d_out = (float *)b_out.p;
+    }
+    if (!offs_dev) {
+        FG_CUDA(b_offs.alloc(off_bytes, s), "alloc offsets");
+        FG_CUDA(cudaMemcpyAsync(b_offs.p, h_offs.data(), off_bytes, cudaMemcpyHostToDevice, s), "offsets H2D");
+        d_offs = (const float *)b_offs.p;
+    }
+    if (algo == FG_ALGO_PIXEL) {
+        FG_CUDA(b_cells.alloc(sizeof(CellParam) * n_in, s), "alloc cell table");
+        FG_CUDA(b_diag.alloc(sizeof(unsigned long long) * 4, s), "alloc diag");
+        FG_CUDA(cudaMemsetAsync(b_diag.p, 0, sizeof(unsigned long long) * 4, s), "memset diag");
+        st = enqueue_pixelwise(d_lam, p, d, h_offs.data(), d_offs, d_out, (CellParam *)b_cells.p,
+                               (unsigned long long *)b_diag.p, nullptr, s);
+    } else {
+        GrainwiseArgs a = grainwise_args(p, d, h_offs.data(), d_lam, d_offs, d_out);
+        st = enqueue_grainwise(a, s);
+    }
+    if (st != FG_OK) {
+        cudaStreamSynchronize(s);
+        return st;
+    }
+    if (!out_dev) FG_CUDA(cudaMemcpyAsync(out, d_out, sizeof(float) * n_out, cudaMemcpyDeviceToHost, s), "out D2H");
+    if (algo == FG_ALGO_PIXEL)
+        FG_CUDA(cudaMemcpyAsync(g_pw_diag, b_diag.p, sizeof g_pw_diag, cudaMemcpyDeviceToHost, s), "diag D2H");
+    FG_CUDA(cudaStreamSynchronize(s), "render");
+    if (cancelled(cancel)) return set_error(FG_ERR_CANCELLED, "cancelled");
+    clear_error();
+    return FG_OK;
+}
+
+}  // namespace fg
+
+using namespace fg;
+
+extern "C" {
+
+FG_API fg_status fg_render_pixelwise(const float *lambda, const fg_params *params, const fg_derived *derived,
+                                     const float *offsets_input, float *out, const volatile int32_t *cancel,
+                                     void *stream) {
+    return render_plane_sync(FG_ALGO_PIXEL, lambda, params, derived, offsets_input, out, cancel, stream);
+}
+
+FG_API fg_status fg_render_grainwise(const float *lambda, const fg_params *params, const fg_derived *derived,
+                                     const float *offsets, float *out, const volatile int32_t *cancel, void *stream) {
+    return render_plane_sync(FG_ALGO_GRAIN, lambda, params, derived, offsets, out, cancel, stream);
+}
+
+FG_API fg_status fg_render_pixelwise_async(const float *d_lambda, const fg_params *params, const fg_derived *derived,
+                                           const float *offsets_input, float *d_out, void *stream) {
+    fg_status st = check_common(params, derived);
+    if (st != FG_OK) return st;
+    if (!d_lambda || !offsets_input || !d_out) return set_error(FG_ERR_INVALID, "null buffer");
+    if (is_device_ptr(offsets_input)) return set_error(FG_ERR_INVALID, "offsets_input must be host memory");
+    keep_pool_memory();
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t n_in = (size_t)derived->input_width * derived->input_height;
+    const size_t off_bytes = sizeof(float) * 2 * params->n_samples;
+    DevBuf b_offs, b_cells, b_diag;
+    FG_CUDA(b_offs.alloc(off_bytes, s), "alloc offsets");
+    FG_CUDA(cudaMemcpyAsync(b_offs.p, offsets_input, off_bytes, cudaMemcpyHostToDevice, s), "offsets H2D");
+    FG_CUDA(b_cells.alloc(sizeof(CellParam) * n_in, s), "alloc cell table");
+    FG_CUDA(b_diag.alloc(sizeof(unsigned long long) * 4, s), "alloc diag");
+    FG_CUDA(cudaMemsetAsync(b_diag.p, 0, sizeof(unsigned long long) * 4, s), "memset diag");
+    return enqueue_pixelwise(d_lambda, *params, *derived, offsets_input, (const float *)b_offs.p, d_out,
+                             (CellParam *)b_cells.p, (unsigned long long *)b_diag.p, nullptr, s);
+}
+
+FG_API fg_status fg_render_grainwise_async(const float *d_lambda, const fg_params *params, const fg_derived *derived,
+                                           const float *offsets, float *d_out, void *stream) {
+    fg_status st = check_common(params, derived);
+    if (st != FG_OK) return st;
+    if (!d_lambda || !offsets || !d_out) return set_error(FG_ERR_INVALID, "null buffer");
+    if (is_device_ptr(offsets)) return set_error(FG_ERR_INVALID, "offsets must be host memory");
+    keep_pool_memory();
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t off_bytes = sizeof(float) * 2 * params->n_samples;
+    DevBuf b_offs;
+    FG_CUDA(b_offs.alloc(off_bytes, s), "alloc offsets");
+    FG_CUDA(cudaMemcpyAsync(b_offs.p, offsets, off_bytes, cudaMemcpyHostToDevice, s), "offsets H2D");
+    GrainwiseArgs a = grainwise_args(*params, *derived, offsets, d_lambda, (const float *)b_offs.p, d_out);
+    return enqueue_grainwise(a, s);
+}
+
+FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height, const fg_params *params,
+                                 uint8_t *out_rgb8, fg_render_stats *stats, const volatile int32_t *cancel,
+                                 void *stream) {
+    if (!rgb || !params || !out_rgb8) return set_error(FG_ERR_INVALID, "null pointer");
+    if (width <= 0 || height <= 0) return set_error(FG_ERR_INVALID, "input image is empty");
+    if (cancelled(cancel)) return set_error(FG_ERR_CANCELLED, "cancelled");
+    const fg_params &p = *params;
+    int64_t x0 = 0, y0 = 0, cw = width, ch = height;
+    if (p.has_roi) {
+        if ((int64_t)p.roi_x1 > width || (int64_t)p.roi_y1 > height)
+            return set_error(FG_ERR_INVALID, "ROI exceeds image bounds");
+        x0 = p.roi_x0; y0 = p.roi_y0;
+        cw = (int64_t)p.roi_x1 - p.roi_x0; ch = (int64_t)p.roi_y1 - p.roi_y0;
+        if (cw <= 0 || ch <= 0) return set_error(FG_ERR_INVALID, "ROI width and height must be positive");
+    }
+    fg_derived d;
+    std::vector<float> offs(2 * (size_t)p.n_samples), offs_in(2 * (size_t)p.n_samples);
+    fg_status st = derive(p, cw, ch, &d, offs.data(), offs_in.data());
+    if (st != FG_OK) return st;
+    st = check_common(params, &d);
+    if (st != FG_OK) return st;
+    const int32_t algo = choose_algorithm(p, d);
+    const bool luma = p.color_mode == FG_COLOR_LUMA;
+    const int nplanes = luma ? 1 : 3;
+    const size_t n_in = (size_t)cw * ch, n_out = (size_t)d.output_width * d.output_height;
+
+    std::vector<float> planes(3 * n_in);
+    split_planes(rgb, width, x0, y0, cw, ch, luma ? 1 : 0, planes.data(), planes.data() + n_in,
+                 planes.data() + 2 * n_in);
+    if (cancelled(cancel)) return set_error(FG_ERR_CANCELLED, "cancelled");
+
+    keep_pool_memory();
+    cudaStream_t s = (cudaStream_t)stream;
+    DevBuf b_lam, b_out, b_rgb8, b_cbcr, b_offs, b_cells, b_diag;
+    FG_CUDA(b_lam.alloc(sizeof(float) * n_in * nplanes, s), "alloc lambda");
+    FG_CUDA(b_out.alloc(sizeof(float) * n_out * nplanes, s), "alloc planes");
+    FG_CUDA(b_rgb8.alloc(3 * n_out, s), "alloc rgb8");
+    FG_CUDA(b_offs.alloc(sizeof(float) * 2 * p.n_samples, s), "alloc offsets");
+    const float *h_offs_used = algo == FG_ALGO_PIXEL ? offs_in.data() : offs.data();
+    FG_CUDA(cudaMemcpyAsync(b_offs.p, h_offs_used, sizeof(float) * 2 * p.n_samples, cudaMemcpyHostToDevice, s),
+            "offsets H2D");
+    float *d_lam = (float *)b_lam.p, *d_out = (float *)b_out.p;
+    float *d_cb = nullptr, *d_cr = nullptr;
+    if (luma) {
+        FG_CUDA(b_cbcr.alloc(sizeof(float) * 2 * n_in, s), "alloc chroma");
+        d_cb = (float *)b_cbcr.p;
+        d_cr = d_cb + n_in;
+        FG_CUDA(cudaMemcpyAsync(d_cb, planes.data() + n_in, sizeof(float) * 2 * n_in, cudaMemcpyHostToDevice, s),
+                "chroma H2D");
+    }
+    if (algo == FG_ALGO_PIXEL) {
+        FG_CUDA(b_cells.alloc(sizeof(CellParam) * n_in, s), "alloc cell table");
+        FG_CUDA(b_diag.alloc(sizeof(unsigned long long) * 4, s), "alloc diag");
+        FG_CUDA(cudaMemsetAsync(b_diag.p, 0, sizeof(unsigned long long) * 4, s), "memset diag");
+    }
+    std::vector<float> norm(n_in), lam((size_t)n_in * nplanes);
+    for (int c = 0; c < nplanes; c++) {
+        if (cancelled(cancel)) {
+            cudaStreamSynchronize(s);
+            return set_error(FG_ERR_CANCELLED, "cancelled");
+        }
+        float *lc = lam.data() + (size_t)c * n_in;
+        normalize_plane(planes.data() + (size_t)c * n_in, (int64_t)n_in, norm.data());
+        lambda_plane(norm.data(), (int64_t)n_in, d.inv_e_pi_r2, lc);
+        FG_CUDA(cudaMemcpyAsync(d_lam + (size_t)c * n_in, lc, sizeof(float) * n_in, cudaMemcpyHostToDevice, s),
+                "lambda H2D");
+        float *d_plane = d_out + (size_t)c * n_out;
+        if (algo == FG_ALGO_PIXEL) {
+            EpilogueArgs e;
+            std::memset(&e, 0, sizeof e);
+            if (luma) {
+                e.mode = 1; e.out_rgb8 = (unsigned char *)b_rgb8.p; e.cb = d_cb; e.cr = d_cr;
+            } else if (c == 2) {
+                e.mode = 2; e.out_rgb8 = (unsigned char *)b_rgb8.p; e.p0 = d_out; e.p1 = d_out + n_out;
+            }
+            st = enqueue_pixelwise(d_lam + (size_t)c * n_in, p, d, offs_in.data(), (const float *)b_offs.p, d_plane,
+                                   (CellParam *)b_cells.p, (unsigned long long *)b_diag.p, &e, s);
+        } else {
+            GrainwiseArgs a = grainwise_args(p, d, offs.data(), d_lam + (size_t)c * n_in, (const float *)b_offs.p,
+                                             d_plane);
+            if (luma) {
+                a.out_rgb8 = (unsigned char *)b_rgb8.p;
+                a.cb = d_cb;
+                a.cr = d_cr;
+            }
+            st = enqueue_grainwise(a, s);
+            if (st == FG_OK && !luma && c == 2) {
+                cudaError_t e = launch_rgb_pack(d_out, d_out + n_out, d_out + 2 * n_out, (int)n_out,
+                                                (unsigned char *)b_rgb8.p, s);
+                if (e != cudaSuccess) st = cuda_error(e, "rgb pack");
+            }
+        }
+        if (st != FG_OK) {
+            cudaStreamSynchronize(s);
+            return st;
+        }
+    }
+    FG_CUDA(cudaMemcpyAsync(out_rgb8, b_rgb8.p, 3 * n_out, cudaMemcpyDeviceToHost, s), "rgb8 D2H");
+    FG_CUDA(cudaStreamSynchronize(s), "render");
+    if (cancelled(cancel)) return set_error(FG_ERR_CANCELLED, "cancelled");
+    if (stats) fill_stats(p, d, algo, stats);
+    clear_error();
+    return FG_OK;
+}
+
+// Counters of the calling thread's last synchronous pixel-wise render: samples evaluated on the
+// per-sample regeneration path, blocks without a staged window, block subdivisions, blocks run.
+FG_API void fg_pixelwise_diagnostics(unsigned long long out[4]) {
+    for (int i = 0; i < 4; i++) out[i] = g_pw_diag[i];
+}
+
+}  // extern "C"

@@ -1,0 +1,27 @@
+// fg_internal.h -- planning and enqueue helpers shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include "../../include/film_grain_gb300.h"
+#include "fg_kernels.cuh"
+
+namespace fg {
+
+// Pixel-wise launch plan: block edge (input pixels, a power of two), block grid and offset extents.
+struct PwPlan {
+    float bsize;
+    int bx0, by0, nbx, nby;
+    float ext[4];  // offset x min, x max, y min, y max
+};
+
+fg_status cuda_error(cudaError_t e, const char *what);
+bool is_device_ptr(const void *p);
+void offset_extents(const float *offs, uint32_t n, float ext[4]);
+PwPlan plan_pixelwise(const fg_params &p, const fg_derived &d, const float *h_offs_in);
+fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_derived &d, const float *h_offs_in,
+                            const float *d_offs_in, float *d_out, CellParam *d_cells, unsigned long long *d_diag,
+                            const EpilogueArgs *colour, cudaStream_t s);
+GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const float *h_offs, const float *d_lam,
+                             const float *d_offs, float *d_out);
+fg_status enqueue_grainwise(const GrainwiseArgs &a, cudaStream_t s);
+
+}  // namespace fg

@@ -1,0 +1,83 @@
+// fg_kernels.cuh -- launch descriptors shared by the kernels and the C-ABI layer.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace fg {
+
+// Per input pixel: the Poisson set-up of a pixel-wise cell whose lambda lookup lands on the pixel
+// (src/pixelwise.rs:69-82).  `thresh` turns the first Knuth comparison into an integer test on the
+// first draw's 53-bit value v: U1 = v * 2^-53 > exp_lambda  <=>  v > floor(exp_lambda * 2^53), so
+// v <= thresh means q = 0.  thresh = INT64_MAX means "no grains" (lambda <= 0 or
+// lambda*delta*delta <= 0, the cell is skipped without drawing); thresh = -1 marks the rejection
+// regime (lambda*delta^2 >= 12), where exp_lambda holds -expected.
+struct __align__(16) CellParam {
+    long long thresh;
+    double exp_lambda;
+};
+
+// Shared-memory capacities of the pixel-wise tile kernel.
+constexpr int kPwThreads = 512;
+constexpr int kPwCellMax = 8192;   // staged window cells
+constexpr int kPwGrainMax = 4096;  // staged grains (16 B each)
+constexpr int kPwEdgeMax = 128;    // window cells per axis
+constexpr int kPwKChunk = 256;     // offsets per sample-assignment chunk
+constexpr int kPwFootMax = 1024;   // per-block output-pixel counters
+constexpr int kPwMaxLevel = 3;     // block subdivision depth on grain overflow
+
+struct PixelwiseArgs {
+    const float *lam;           // in_w x in_h
+    const CellParam *cells;     // in_w x in_h
+    const float2 *offs;         // offsets_input [n]
+    float *out;                 // out_w x out_h, accumulates hit counts (pre-zeroed)
+    unsigned long long *diag;   // [4] counters: slow samples, overflow blocks, subdivisions, blocks
+    int in_w, in_h, out_w, out_h;
+    int n;
+    float rm, delta, inv_zoom, zoom;
+    float bsize, inv_bsize;     // block edge in input pixels (power of two) and its inverse
+    int bx0, by0, nbx;          // block-grid origin and width
+    float offx_min, offx_max, offy_min, offy_max;
+    unsigned long long seed;
+    int lognorm;
+    float radius_mean;
+    double log_mu, log_sigma;
+};
+
+struct GrainwiseArgs {
+    const float *lam;           // in_w x in_h
+    const float2 *offs;         // offsets (output pixels) [n]
+    float *out;                 // out_w x out_h f32 plane (may be null when out_rgb8 is used)
+    unsigned char *out_rgb8;    // fused colour output (luma mode) or null
+    const float *cb, *cr;       // luma mode: chroma planes at input size
+    int in_w, in_h, out_w, out_h;
+    int n, words;               // words = ceil(n/32)
+    int tile_w, tile_h;
+    float rm, zoom;
+    float offx_min, offx_max, offy_min, offy_max;
+    unsigned long long seed;
+    int lognorm;
+    float radius_mean;
+    double log_mu, log_sigma;
+};
+
+// Epilogue of the pixel-wise path: counts -> value (and optional colour packing).
+struct EpilogueArgs {
+    float *plane;               // counts in, values out (in place)
+    int out_w, out_h, in_w, in_h;
+    float inv_samples;
+    unsigned char *out_rgb8;    // null: values only
+    int mode;                   // 0 values, 1 luma recombine, 2 rgb pack (plane is channel 2)
+    const float *cb, *cr;       // luma: chroma planes at input size
+    const float *p0, *p1;       // rgb: rendered channels 0 and 1 (values)
+};
+
+cudaError_t launch_cell_params(const float *lam, int in_w, int in_h, float delta, CellParam *cells, cudaStream_t s);
+cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, size_t smem, cudaStream_t s);
+size_t pixelwise_smem_bytes();
+cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s);
+size_t grainwise_smem_bytes(const GrainwiseArgs &a);
+cudaError_t launch_epilogue(const EpilogueArgs &a, cudaStream_t s);
+cudaError_t launch_rgb_pack(const float *p0, const float *p1, const float *p2, int n, unsigned char *out,
+                            cudaStream_t s);
+
+}  // namespace fg

@@ -1,0 +1,351 @@
+// fg_rng.cuh -- the film_grain RNG streams and samplers, bit-identical on host and device.
+//
+// Restates src/rng.rs:1-52 and the third-party samplers it calls:
+//   rand 0.8.5     SmallRng = xoshiro256++ seeded by SplitMix64; next_u32 = high half of next_u64;
+//                  UniformFloat<f32> (23-bit mantissa draw); Standard f64 (53-bit multiply method);
+//                  Open01 f64 (52-bit transmute method).
+//   rand_core 0.6  SeedableRng::seed_from_u64 default (PCG32 output words fill the seed), used by
+//                  StdRng::seed_from_u64 in make_offsets (src/rng.rs:15).
+//   rand_chacha    ChaCha12Rng = StdRng: ChaCha block function, 12 rounds, 64-bit counter, stream 0.
+//   rand_distr 0.4.3  Poisson (Knuth product below lambda 12, Cauchy-comparison rejection above,
+//                  Numerical Recipes' log-gamma), Normal via the 256-layer ziggurat, LogNormal.
+// Every floating-point operation on the coverage path is an explicit round-to-nearest intrinsic on
+// the device (no FMA contraction), matching Rust's unfused expression order.
+#pragma once
+#include <stdint.h>
+#include <math.h>
+#include "zig_tables.h"
+
+#if defined(__CUDACC__)
+#define FG_HD __host__ __device__ __forceinline__
+#else
+#define FG_HD inline
+#endif
+
+#ifdef __CUDA_ARCH__
+#define FG_FMUL(a, b) __fmul_rn((a), (b))
+#define FG_FADD(a, b) __fadd_rn((a), (b))
+#define FG_FSUB(a, b) __fsub_rn((a), (b))
+#define FG_FDIV(a, b) __fdiv_rn((a), (b))
+#define FG_DMUL(a, b) __dmul_rn((a), (b))
+#define FG_DADD(a, b) __dadd_rn((a), (b))
+#define FG_DSUB(a, b) __dsub_rn((a), (b))
+#define FG_DDIV(a, b) __ddiv_rn((a), (b))
+#else
+#define FG_FMUL(a, b) ((float)(a) * (float)(b))
+#define FG_FADD(a, b) ((float)(a) + (float)(b))
+#define FG_FSUB(a, b) ((float)(a) - (float)(b))
+#define FG_FDIV(a, b) ((float)(a) / (float)(b))
+#define FG_DMUL(a, b) ((double)(a) * (double)(b))
+#define FG_DADD(a, b) ((double)(a) + (double)(b))
+#define FG_DSUB(a, b) ((double)(a) - (double)(b))
+#define FG_DDIV(a, b) ((double)(a) / (double)(b))
+#endif
+
+namespace fg {
+
+constexpr uint64_t kPhi = 0x9E3779B97F4A7C15ull;
+constexpr uint64_t kOffsetStream = 0x9E3779B97F4A7C15ull;  // src/rng.rs:5
+constexpr uint64_t kCellStream = 0xA24B1C30BEBCCF59ull;    // src/rng.rs:6
+constexpr uint64_t kPixelStream = 0x6935FA5C55F65F1Bull;   // src/rng.rs:7
+
+FG_HD uint64_t rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+// The SplitMix64 output function.
+FG_HD uint64_t fmix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+// src/rng.rs:46-52
+FG_HD uint64_t splitmix64(uint64_t x) { return fmix64(x + kPhi); }
+// src/rng.rs:40-44 (i64 -> u64 reinterpretation, wrapping adds, rotations 17 and 41)
+FG_HD uint64_t mix3(uint64_t seed, uint64_t stream, int64_t a, int64_t b) {
+    uint64_t st = seed ^ stream;
+    st = splitmix64(rotl64(st + (uint64_t)a, 17));
+    return splitmix64(rotl64(st + (uint64_t)b, 41));
+}
+
+// xoshiro256++ (rand 0.8.5 SmallRng on 64-bit targets).
+struct Xoshiro {
+    uint64_t s0, s1, s2, s3;
+    FG_HD uint64_t next() {
+        uint64_t r = rotl64(s0 + s3, 23) + s0;
+        uint64_t t = s1 << 17;
+        s2 ^= s0;
+        s3 ^= s1;
+        s1 ^= s2;
+        s0 ^= s3;
+        s2 ^= t;
+        s3 = rotl64(s3, 45);
+        return r;
+    }
+};
+// SmallRng::seed_from_u64: word i = fmix64(h + (i+1)*phi).  The four arguments differ, and fmix64 is
+// a bijection with fmix64(0) = 0, so at most one word can be zero: the all-zero-seed remap of
+// from_seed can never trigger and is omitted.
+FG_HD Xoshiro small_seed(uint64_t h) {
+    Xoshiro x;
+    x.s0 = fmix64(h + kPhi);
+    x.s1 = fmix64(h + 2 * kPhi);
+    x.s2 = fmix64(h + 3 * kPhi);
+    x.s3 = fmix64(h + 4 * kPhi);
+    return x;
+}
+// src/rng.rs:26-29 / 31-34
+FG_HD Xoshiro cell_rng(uint64_t seed, int32_t i, int32_t j) { return small_seed(mix3(seed, kCellStream, i, j)); }
+FG_HD Xoshiro pixel_rng(uint64_t seed, int32_t i, int32_t j) { return small_seed(mix3(seed, kPixelStream, i, j)); }
+
+FG_HD float bits_f32(uint32_t b) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(b);
+#else
+    union { uint32_t u; float f; } c; c.u = b; return c.f;
+#endif
+}
+FG_HD uint32_t f32_bits(float f) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    union { uint32_t u; float f; } c; c.f = f; return c.u;
+#endif
+}
+FG_HD double bits_f64(uint64_t b) {
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    union { uint64_t u; double d; } c; c.u = b; return c.d;
+#endif
+}
+FG_HD uint64_t f64_bits(double d) {
+#ifdef __CUDA_ARCH__
+    return (uint64_t)__double_as_longlong(d);
+#else
+    union { uint64_t u; double d; } c; c.d = d; return c.u;
+#endif
+}
+
+// v * 2^-53 for v < 2^53, built from integer operations only (exact; no FP64 conversion unit).
+FG_HD double u53_unit(uint64_t v) {
+    if (v == 0) return 0.0;
+#ifdef __CUDA_ARCH__
+    int lz = __clzll((long long)v);
+#else
+    int lz = __builtin_clzll(v);
+#endif
+    int e = 63 - lz;  // 0..52
+    uint64_t mant = (v << (52 - e)) & 0x000FFFFFFFFFFFFFull;
+    uint64_t ex = (uint64_t)(1023 - 53 + e);
+    return bits_f64((ex << 52) | mant);
+}
+// Standard f64 from one raw draw.
+FG_HD double std_f64_from(uint64_t raw) { return u53_unit(raw >> 11); }
+// Open01 f64 from one raw draw: [1,2) minus (1 - eps/2).
+FG_HD double open01_from(uint64_t raw) {
+    return FG_DSUB(bits_f64((raw >> 12) | 0x3FF0000000000000ull), 0.99999999999999988897769753748434595763683319091796875);
+}
+
+// UniformFloat<f32> (rand 0.8.5).
+struct UniformF32 {
+    float low, scale;
+};
+FG_HD UniformF32 uniform_f32_new(float low, float high) {
+    const float max_rand = bits_f32(0x3F800000u | (0xFFFFFFFFu >> 9)) - 1.0f;  // 1 - 2^-23, exact
+    float scale = FG_FSUB(high, low);
+    for (int guard = 0; guard < 64; guard++) {
+        float t = FG_FADD(FG_FMUL(scale, max_rand), low);
+        if (!(t >= high)) break;
+        scale = bits_f32(f32_bits(scale) - 1u);
+    }
+    UniformF32 u = {low, scale};
+    return u;
+}
+// One sample from one raw next_u64 draw (next_u32 = high half; 23 high bits of that).
+FG_HD float uniform_f32_from(const UniformF32 &u, uint64_t raw) {
+    uint32_t m = (uint32_t)(raw >> 41);
+    float v01 = FG_FSUB(bits_f32(m | 0x3F800000u), 1.0f);
+    return FG_FADD(FG_FMUL(v01, u.scale), u.low);
+}
+
+// rand_distr::utils::log_gamma: Numerical Recipes' gammln (Lanczos, g = 5, six terms).
+FG_HD double log_gamma(double x) {
+    const double c0 = 76.18009172947146, c1 = -86.50532032941677, c2 = 24.01409824083091,
+                 c3 = -1.231739572450155, c4 = 0.1208650973866179e-2, c5 = -0.5395239384953e-5;
+    double tmp = FG_DADD(x, 5.5);
+    double lg = FG_DSUB(FG_DMUL(FG_DADD(x, 0.5), log(tmp)), tmp);
+    double a = 1.000000000190015;
+    double den = x;
+    den = FG_DADD(den, 1.0); a = FG_DADD(a, FG_DDIV(c0, den));
+    den = FG_DADD(den, 1.0); a = FG_DADD(a, FG_DDIV(c1, den));
+    den = FG_DADD(den, 1.0); a = FG_DADD(a, FG_DDIV(c2, den));
+    den = FG_DADD(den, 1.0); a = FG_DADD(a, FG_DDIV(c3, den));
+    den = FG_DADD(den, 1.0); a = FG_DADD(a, FG_DDIV(c4, den));
+    den = FG_DADD(den, 1.0); a = FG_DADD(a, FG_DDIV(c5, den));
+    return FG_DADD(lg, log(FG_DDIV(FG_DMUL(2.5066282746310005, a), x)));
+}
+
+// Poisson::new (rand_distr 0.4.3).
+struct PoissonParams {
+    double lambda, exp_lambda, log_lambda, sqrt_2lambda, magic_val;
+};
+FG_HD PoissonParams poisson_new(double lambda) {
+    PoissonParams p;
+    p.lambda = lambda;
+    p.log_lambda = log(lambda);
+    p.exp_lambda = exp(-lambda);
+    p.sqrt_2lambda = sqrt(FG_DMUL(2.0, lambda));
+    p.magic_val = FG_DSUB(FG_DMUL(lambda, p.log_lambda), log_gamma(FG_DADD(1.0, lambda)));
+    return p;
+}
+
+// Knuth continuation: p already holds the first uniform and exceeds exp_lambda; returns the count.
+template <class Rng>
+FG_HD uint32_t poisson_knuth_tail(double p, double exp_lambda, Rng &rng) {
+    double result = 2.0;  // result after the first multiplication (1 + 1)
+    p = FG_DMUL(p, std_f64_from(rng.next()));
+    while (p > exp_lambda) {
+        p = FG_DMUL(p, std_f64_from(rng.next()));
+        result = FG_DADD(result, 1.0);
+    }
+    double r = FG_DSUB(result, 1.0);
+    return r >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)r;
+}
+
+// Poisson::sample, rejection branch (lambda >= 12).
+template <class Rng>
+FG_HD uint32_t poisson_rejection(const PoissonParams &P, Rng &rng) {
+    const double kPi = 3.14159265358979323846264338327950288;
+    double result, comp_dev;
+    for (;;) {
+        for (;;) {
+            double x = std_f64_from(rng.next());
+            comp_dev = tan(FG_DMUL(kPi, x));
+            comp_dev = FG_DADD(0.0, FG_DMUL(1.0, comp_dev));  // Cauchy(median 0, scale 1)
+            result = FG_DADD(FG_DMUL(P.sqrt_2lambda, comp_dev), P.lambda);
+            if (result >= 0.0) break;
+        }
+        result = floor(result);
+        double arg = FG_DSUB(FG_DSUB(FG_DMUL(result, P.log_lambda), log_gamma(FG_DADD(1.0, result))), P.magic_val);
+        double check = FG_DMUL(FG_DMUL(0.9, FG_DADD(1.0, FG_DMUL(comp_dev, comp_dev))), exp(arg));
+        if (std_f64_from(rng.next()) <= check) break;
+    }
+    return result >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)result;
+}
+
+// Poisson::sample cast with `as u32`.
+template <class Rng>
+FG_HD uint32_t poisson_sample(const PoissonParams &P, Rng &rng) {
+    if (P.lambda < 12.0) {
+        double p = std_f64_from(rng.next());
+        if (!(p > P.exp_lambda)) return 0;
+        return poisson_knuth_tail(p, P.exp_lambda, rng);
+    }
+    return poisson_rejection(P, rng);
+}
+
+// 256-layer ziggurat tables.
+#ifdef __CUDACC__
+static __device__ const double g_zig_x[257] = FG_ZIG_NORM_X_INIT;
+static __device__ const double g_zig_f[257] = FG_ZIG_NORM_F_INIT;
+#endif
+static const double h_zig_x[257] = FG_ZIG_NORM_X_INIT;
+static const double h_zig_f[257] = FG_ZIG_NORM_F_INIT;
+
+FG_HD double zig_x(unsigned i) {
+#ifdef __CUDA_ARCH__
+    return __ldg(&g_zig_x[i]);
+#else
+    return h_zig_x[i];
+#endif
+}
+FG_HD double zig_f(unsigned i) {
+#ifdef __CUDA_ARCH__
+    return __ldg(&g_zig_f[i]);
+#else
+    return h_zig_f[i];
+#endif
+}
+
+// StandardNormal for f64 (rand_distr 0.4.3 ziggurat, symmetric, 256 layers).
+template <class Rng>
+FG_HD double std_normal(Rng &rng) {
+    for (;;) {
+        uint64_t bits = rng.next();
+        unsigned i = (unsigned)(bits & 0xffu);
+        double u = FG_DSUB(bits_f64((bits >> 12) | 0x4000000000000000ull), 3.0);
+        double x = FG_DMUL(u, zig_x(i));
+        if (fabs(x) < zig_x(i + 1)) return x;
+        if (i == 0) {
+            double xx = 1.0, yy = 0.0;
+            while (FG_DMUL(-2.0, yy) < FG_DMUL(xx, xx)) {
+                double x_ = open01_from(rng.next());
+                double y_ = open01_from(rng.next());
+                xx = FG_DDIV(log(x_), FG_ZIG_NORM_R);
+                yy = log(y_);
+            }
+            return (u < 0.0) ? FG_DSUB(xx, FG_ZIG_NORM_R) : FG_DSUB(FG_ZIG_NORM_R, xx);
+        }
+        double pdf = exp(FG_DDIV(FG_DMUL(-x, x), 2.0));
+        double fi1 = zig_f(i + 1);
+        if (FG_DADD(fi1, FG_DMUL(FG_DSUB(zig_f(i), fi1), std_f64_from(rng.next()))) < pdf) return x;
+    }
+}
+
+// Normal::sample = mean + sd * z.
+template <class Rng>
+FG_HD double normal_sample(double mean, double sd, Rng &rng) {
+    return FG_DADD(mean, FG_DMUL(sd, std_normal(rng)));
+}
+
+// ChaCha12 keystream reader (StdRng), seeded through rand_core's PCG32 seed_from_u64.
+struct ChaCha12 {
+    uint32_t key[8];
+    uint64_t block;
+    uint32_t buf[16];
+    int idx;
+};
+FG_HD uint32_t rotl32(uint32_t x, int k) { return (x << k) | (x >> (32 - k)); }
+FG_HD void chacha_block(const uint32_t key[8], uint64_t counter, uint64_t stream, int rounds, uint32_t out[16]) {
+    uint32_t s[16] = {0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u, key[0], key[1], key[2], key[3],
+                      key[4], key[5], key[6], key[7], (uint32_t)counter, (uint32_t)(counter >> 32),
+                      (uint32_t)stream, (uint32_t)(stream >> 32)};
+    uint32_t x[16];
+    for (int i = 0; i < 16; i++) x[i] = s[i];
+#define FG_QR(a, b, c, d)                                                     \
+    x[a] += x[b]; x[d] = rotl32(x[d] ^ x[a], 16);                            \
+    x[c] += x[d]; x[b] = rotl32(x[b] ^ x[c], 12);                            \
+    x[a] += x[b]; x[d] = rotl32(x[d] ^ x[a], 8);                             \
+    x[c] += x[d]; x[b] = rotl32(x[b] ^ x[c], 7);
+    for (int r = 0; r < rounds; r += 2) {
+        FG_QR(0, 4, 8, 12) FG_QR(1, 5, 9, 13) FG_QR(2, 6, 10, 14) FG_QR(3, 7, 11, 15)
+        FG_QR(0, 5, 10, 15) FG_QR(1, 6, 11, 12) FG_QR(2, 7, 8, 13) FG_QR(3, 4, 9, 14)
+    }
+#undef FG_QR
+    for (int i = 0; i < 16; i++) out[i] = x[i] + s[i];
+}
+FG_HD ChaCha12 chacha12_seed_from_u64(uint64_t state) {
+    ChaCha12 c;
+    for (int i = 0; i < 8; i++) {
+        state = state * 6364136223846793005ull + 11634580027462260723ull;
+        uint32_t xs = (uint32_t)(((state >> 18) ^ state) >> 27);
+        uint32_t rot = (uint32_t)(state >> 59);
+        c.key[i] = rot ? ((xs >> rot) | (xs << (32u - rot))) : xs;
+    }
+    c.block = 0;
+    c.idx = 16;
+    return c;
+}
+struct ChaChaStream {
+    ChaCha12 c;
+    FG_HD uint64_t next() {
+        if (c.idx >= 16) {
+            chacha_block(c.key, c.block++, 0, 12, c.buf);
+            c.idx = 0;
+        }
+        uint64_t lo = c.buf[c.idx], hi = c.buf[c.idx + 1];
+        c.idx += 2;
+        return (hi << 32) | lo;
+    }
+};
+
+}  // namespace fg

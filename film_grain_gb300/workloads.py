@@ -1,0 +1,44 @@
+"""Seeded synthetic inputs with the shapes and value distributions of the benchmark workloads.
+
+No image dataset is involved: each workload is generated from its seed.
+- ramp_noise: horizontal linear ramp 0 -> 1 plus uniform noise +-0.05, clamped to [0, 1]
+  (the 256 x 256 luma pixel-wise workload).
+- blobs: isotropic Gaussian blobs (amplitude U[0.2, 0.9], sigma U[30, 150] px) over a 0.1 background,
+  clamped to [0, 1], each channel seeded independently (the 1024^2 x 3 grain-wise workload and the
+  4096^2 x 3 large-frame workload).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def ramp_noise(width: int = 256, height: int = 256, seed: int = 42) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    ramp = np.linspace(0.0, 1.0, width, dtype=np.float64)[None, :].repeat(height, 0)
+    v = ramp + rng.uniform(-0.05, 0.05, size=(height, width))
+    return np.clip(v, 0.0, 1.0).astype(np.float32)
+
+
+def blobs_plane(width: int, height: int, seed: int, n_blobs: int = 16, background: float = 0.1) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    amp = rng.uniform(0.2, 0.9, n_blobs)
+    sig = rng.uniform(30.0, 150.0, n_blobs)
+    cx = rng.uniform(0, width, n_blobs)
+    cy = rng.uniform(0, height, n_blobs)
+    xs = np.arange(width, dtype=np.float64) + 0.5
+    ys = np.arange(height, dtype=np.float64) + 0.5
+    v = np.full((height, width), background, np.float64)
+    for a, s, x0, y0 in zip(amp, sig, cx, cy):
+        gx = np.exp(-((xs - x0) ** 2) / (2 * s * s))
+        gy = np.exp(-((ys - y0) ** 2) / (2 * s * s))
+        v += a * gy[:, None] * gx[None, :]
+    return np.clip(v, 0.0, 1.0).astype(np.float32)
+
+
+def blobs_rgb(width: int, height: int, seed: int) -> np.ndarray:
+    """(H, W, 3) f32 RGB, each channel an independently seeded blob plane."""
+    return np.stack([blobs_plane(width, height, seed * 3 + c) for c in range(3)], axis=-1)
+
+
+def gray_rgb(plane: np.ndarray) -> np.ndarray:
+    return np.repeat(plane[:, :, None], 3, axis=2).astype(np.float32)

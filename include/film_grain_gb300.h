@@ -1,0 +1,202 @@
+/*
+ * film_grain_gb300.h -- C-ABI of the GB300 (sm_103a) film-grain integrators.
+ *
+ * A drop-in for the CPU hot path of joseph-wardle/film_grain (Rust crate film_grain 0.1.1): the
+ * pixel-wise and grain-wise Monte Carlo integrators, the deterministic RNG streams they consume,
+ * and the host arithmetic the crate's render entry points run around them.  Coverage counts are
+ * bit-identical to the crate's CPU path on the same inputs and seed.
+ *
+ * Conventions
+ *   - Plain C types only: no CUDA or torch types cross this boundary.  `stream` is a cudaStream_t
+ *     passed as void* (NULL = the legacy default stream).
+ *   - Planes are row-major f32, width x height, no padding.  Offsets are [n][2] f32 (x, y).
+ *   - Pointers may be host or device memory; the library detects which.  Every render call is
+ *     synchronous on return when any of its buffers is host memory; the *_async variants take
+ *     device pointers only and return after enqueueing on `stream`.
+ *   - Every call returns an fg_status; fg_last_error_message() gives the thread's last message.
+ *   - `cancel` (may be NULL) is polled before and between kernel launches; a non-zero value makes
+ *     the call return FG_ERR_CANCELLED (the crate's RenderError::Cancelled, src/lib.rs:41).
+ *   - Thread safety: calls on different streams may run concurrently; the library keeps no state
+ *     but a per-device cache of launch limits and the thread-local error message.
+ */
+#ifndef FILM_GRAIN_GB300_H
+#define FILM_GRAIN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define FG_API __attribute__((visibility("default")))
+#else
+#define FG_API
+#endif
+
+/* RenderError (src/lib.rs:28-44) mapped to status codes. */
+typedef enum fg_status {
+    FG_OK = 0,
+    FG_ERR_PARAMS = 1,      /* RenderError::Params(ParamsError) */
+    FG_ERR_CANCELLED = 2,   /* RenderError::Cancelled */
+    FG_ERR_CUDA = 3,        /* RenderError::Gpu(String) */
+    FG_ERR_INVALID = 4,     /* RenderError::Message: bad sizes, null pointers, empty input */
+    FG_ERR_UNSUPPORTED = 5, /* RenderError::Unsupported */
+    FG_ERR_NOMEM = 6,       /* device allocation failed */
+    FG_ERR_INTERNAL = 7     /* a kernel reported an inconsistent state (never expected) */
+} fg_status;
+
+/* Enums of src/params.rs:6-28. */
+typedef enum fg_radius_dist { FG_RADIUS_CONST = 0, FG_RADIUS_LOGNORM = 1 } fg_radius_dist;
+typedef enum fg_algo { FG_ALGO_AUTO = 0, FG_ALGO_GRAIN = 1, FG_ALGO_PIXEL = 2 } fg_algo;
+typedef enum fg_color_mode { FG_COLOR_LUMA = 0, FG_COLOR_RGB = 1 } fg_color_mode;
+typedef enum fg_max_radius_kind { FG_MAXR_ABSOLUTE = 0, FG_MAXR_QUANTILE = 1 } fg_max_radius_kind;
+
+/* ParamsBuilder (src/params.rs:70-91) without the path / output-format / CLI-only fields. */
+typedef struct fg_params_builder {
+    int32_t radius_dist;      /* fg_radius_dist */
+    float radius_mean;        /* mu_r, input pixels */
+    float radius_stddev;      /* sigma_r, input pixels (lognorm only) */
+    float zoom;               /* output scale s */
+    float sigma_px;           /* Gaussian filter sigma, output pixels */
+    uint32_t n_samples;       /* N (0 is raised to 1, as ParamsBuilder::build does) */
+    int32_t algo;             /* fg_algo */
+    int32_t max_radius_kind;  /* fg_max_radius_kind */
+    float max_radius_value;   /* absolute radius or quantile p in (0,1) */
+    float cell_delta;         /* <= 0 or NaN: None -> default_cell_delta(radius_mean) */
+    int32_t color_mode;       /* fg_color_mode */
+    int32_t has_roi;          /* crop [roi_x0, roi_x1) x [roi_y0, roi_y1) of the input (before zoom) */
+    uint32_t roi_x0, roi_y0, roi_x1, roi_y1;
+    uint32_t size_w, size_h;  /* forced output size; size_w == 0: none; size_h == 0: keep aspect */
+    uint64_t seed;
+} fg_params_builder;
+
+/* Params (src/params.rs:45-68), resolved by ParamsBuilder::build. */
+typedef struct fg_params {
+    int32_t radius_dist;
+    float radius_mean;
+    float radius_stddev;      /* 0 for Const (derive_radius_parameters) */
+    float radius_log_mu;      /* valid when has_log_params */
+    float radius_log_sigma;
+    int32_t has_log_params;
+    float zoom;
+    float sigma_px;
+    uint32_t n_samples;
+    int32_t algo;
+    int32_t max_radius_kind;
+    float max_radius_value;
+    float cell_delta;         /* always resolved (Some) after build */
+    int32_t color_mode;
+    int32_t has_roi;
+    uint32_t roi_x0, roi_y0, roi_x1, roi_y1;
+    uint32_t size_w, size_h;
+    uint64_t seed;
+} fg_params;
+
+/* Derived (src/model.rs:167-179) minus its Vecs: offsets live in caller-owned [n][2] buffers. */
+typedef struct fg_derived {
+    int64_t input_width, input_height;
+    int64_t output_width, output_height;
+    float inv_e_pi_r2;
+    float rm;
+    float delta;
+    uint32_t n_offsets;
+} fg_derived;
+
+/* RenderStats (src/lib.rs:46-55). */
+typedef struct fg_render_stats {
+    int32_t algorithm;        /* FG_ALGO_GRAIN or FG_ALGO_PIXEL */
+    int64_t input_width, input_height, output_width, output_height;
+    uint32_t n_samples;
+    float sigma_ratio;
+    float rm_ratio;
+} fg_render_stats;
+
+/* ---------------------------------------------------------------------------------------------
+ * Host-side parameter resolution (no GPU needed).
+ * ------------------------------------------------------------------------------------------- */
+
+/* ParamsBuilder::build (src/params.rs:141-179): validation plus the lognormal mu/sigma
+ * derivation (src/params.rs:223-253).  FG_ERR_PARAMS with the field named in the message. */
+FG_API fg_status fg_params_build(const fg_params_builder *builder, fg_params *out);
+
+/* derive_common (src/model.rs:181-226): sizes, inv_e_pi_r2, rm, delta and make_offsets
+ * (src/rng.rs:9-24).  offsets / offsets_input receive [n_samples][2] f32 (host memory, may be NULL). */
+FG_API fg_status fg_derive(const fg_params *params, int64_t input_width, int64_t input_height,
+                           fg_derived *out, float *offsets, float *offsets_input);
+
+/* choose_algorithm (src/choose.rs:4-26): FG_ALGO_PIXEL or FG_ALGO_GRAIN. */
+FG_API int32_t fg_choose_algorithm(const fg_params *params, const fg_derived *derived);
+
+/* default_cell_delta (src/params.rs:255-261). */
+FG_API float fg_default_cell_delta(float radius_mean);
+
+/* normalize_plane (src/model.rs:228-250); returns the plane maximum.  Host buffers. */
+FG_API float fg_normalize_plane(const float *src, int64_t n, float *dst);
+
+/* lambda_plane (src/model.rs:252-265).  Host buffers (the crate computes lambda on the host with
+ * the platform logf; so does this library, to stay bit-identical). */
+FG_API void fg_lambda_plane(const float *normalized, int64_t n, float inv_e_pi_r2, float *dst);
+
+/* ---------------------------------------------------------------------------------------------
+ * The integrators.
+ * ------------------------------------------------------------------------------------------- */
+
+/* render_pixelwise (src/pixelwise.rs:11-45): per output pixel, the fraction of the N offset
+ * samples (offsets_input, input-pixel units) covered by a grain of the cell-seeded Boolean model.
+ * lambda: input_width x input_height; out: output_width x output_height. */
+FG_API fg_status fg_render_pixelwise(const float *lambda, const fg_params *params, const fg_derived *derived,
+                                     const float *offsets_input, float *out, const volatile int32_t *cancel,
+                                     void *stream);
+
+/* render_grainwise (src/grainwise.rs:12-124): per output pixel, popcount of the N-bit sample mask
+ * that the pixel-seeded grains' offset disks (offsets, output-pixel units) set, times 1/N. */
+FG_API fg_status fg_render_grainwise(const float *lambda, const fg_params *params, const fg_derived *derived,
+                                     const float *offsets, float *out, const volatile int32_t *cancel,
+                                     void *stream);
+
+/* Device-pointer variants: enqueue on `stream` and return (no host synchronisation). */
+FG_API fg_status fg_render_pixelwise_async(const float *d_lambda, const fg_params *params,
+                                           const fg_derived *derived, const float *d_offsets_input,
+                                           float *d_out, void *stream);
+FG_API fg_status fg_render_grainwise_async(const float *d_lambda, const fg_params *params,
+                                           const fg_derived *derived, const float *d_offsets, float *d_out,
+                                           void *stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Whole-image orchestration (render_with_input_image, src/lib.rs:78-84 / 134-173).
+ * ------------------------------------------------------------------------------------------- */
+
+/* rgb: interleaved f32 RGB, height x width x 3 (what image::to_rgb32f yields; host memory); the
+ * params' ROI, when set, is cropped first (apply_roi, src/color.rs:215-231).
+ * out_rgb8: output_height x output_width x 3 u8 (host memory), sized from fg_dry_run or fg_derive.
+ * Luma mode renders Y only and recombines it with nearest-resized Cb/Cr; RGB mode renders the three
+ * planes with the same seed.  The colour recombination and u8 packing run fused on the GPU. */
+FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height, const fg_params *params,
+                                 uint8_t *out_rgb8, fg_render_stats *stats, const volatile int32_t *cancel,
+                                 void *stream);
+
+/* dry_run_with_input_image (src/lib.rs:100-104): derive + choose only. */
+FG_API fg_status fg_dry_run(int64_t width, int64_t height, const fg_params *params, fg_render_stats *stats);
+
+/* ---------------------------------------------------------------------------------------------
+ * Diagnostics.
+ * ------------------------------------------------------------------------------------------- */
+
+/* Last error message of the calling thread ("" if none). */
+FG_API const char *fg_last_error_message(void);
+
+/* Counters of the calling thread's last synchronous fg_render_pixelwise: [0] samples evaluated on the
+ * per-sample regeneration path, [1] blocks without a staged cell window, [2] block subdivisions on
+ * shared-memory overflow, [3] blocks processed.  No counterpart in the crate (diagnostics only). */
+FG_API void fg_pixelwise_diagnostics(unsigned long long out[4]);
+
+/* Library version string. */
+FG_API const char *fg_version(void);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* FILM_GRAIN_GB300_H */

@@ -1,0 +1,186 @@
+"""GPU parity: the sm_103a integrators against the CPU oracle, bit for bit.
+
+Every case renders the same seeded plane through the library's C-ABI (host lambda plane -> GPU
+integrator) and through the oracle (a C restatement of src/pixelwise.rs / src/grainwise.rs), and
+requires the f32 output planes to be bit-identical (coverage counts equal, the same count * (1/N)).
+"""
+import numpy as np
+import pytest
+
+from film_grain_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(fgl, orc, plane, radius=0.1, dist="const", sd=0.0, zoom=1.0, n=32, seed=5489, sigma=0.8,
+           cell=None, maxr=None, size=None):
+    h, w = plane.shape
+    kw = dict(radius_mean=radius, radius_dist=fgl.RadiusDist.Lognorm if dist == "lognorm" else fgl.RadiusDist.Const,
+              radius_stddev=sd, zoom=zoom, n_samples=n, seed=seed, sigma_px=sigma, cell_delta=cell, size=size)
+    if maxr is not None:
+        kw["max_radius"] = fgl.MaxRadius.Absolute(maxr)
+    p = fgl.ParamsBuilder(**kw).build()
+    d = fgl.derive_common(p, (w, h))
+    norm, _ = fgl.normalize_plane(plane)
+    lam = fgl.lambda_plane(norm, d.inv_e_pi_r2)
+    op = orc.params_struct(dist, radius, sd, zoom, sigma, n, seed)
+    od, offs, offs_in = orc.derive(op, w, h, ("absolute", maxr) if maxr is not None else ("quantile", 0.999), cell,
+                                   size)
+    onorm, _ = orc.normalize_plane(plane)
+    olam = orc.lambda_plane(onorm, od.inv_e_pi_r2)
+    assert np.array_equal(lam.view(np.uint32), olam.view(np.uint32)), "lambda planes differ"
+    assert np.array_equal(d.offsets, offs) and np.array_equal(d.offsets_input, offs_in)
+    assert (d.output_width, d.output_height, d.rm, d.delta) == (od.out_w, od.out_h, od.rm, od.delta)
+    return p, d, lam, op, od, offs, offs_in
+
+
+def _check(algo, fgl, orc, plane, **kw):
+    p, d, lam, op, od, offs, offs_in = _setup(fgl, orc, plane, **kw)
+    if algo == "pixel":
+        got = fgl.render_pixelwise(lam, p, d)
+        want, _ = orc.render("pixel", lam, op, od, offs_in)
+    else:
+        got = fgl.render_grainwise(lam, p, d)
+        want, _ = orc.render("grain", lam, op, od, offs)
+    assert got.shape == want.shape
+    diff = np.count_nonzero(got.view(np.uint32) != want.view(np.uint32))
+    assert diff == 0, f"{diff} of {got.size} pixels differ (max abs {np.abs(got - want).max()})"
+    return got
+
+
+def _blobs(w, h, seed=11):
+    return workloads.blobs_plane(w, h, seed)
+
+
+# ------------------------------------------------------------------ pixel-wise
+def test_pixelwise_ramp_256_n64(cuda, fgl, orc):
+    """The 256x256 luma ramp workload: const radius 0.12, N=64, zoom 1, seed 42."""
+    out = _check("pixel", fgl, orc, workloads.ramp_noise(256, 256, 42), radius=0.12, n=64, seed=42)
+    slow, unstaged, subdiv, blocks = fgl.pixelwise_diagnostics()
+    assert unstaged == 0 and slow == 0 and blocks > 0
+    assert abs(float(out.mean()) - 0.5) < 0.01
+
+
+@pytest.mark.parametrize("n", [1, 7, 37, 100])
+def test_pixelwise_sample_counts(cuda, fgl, orc, n):
+    _check("pixel", fgl, orc, _blobs(48, 40), radius=0.1, n=n, seed=3)
+
+
+def test_pixelwise_lognormal(cuda, fgl, orc):
+    _check("pixel", fgl, orc, _blobs(64, 48), radius=0.05, dist="lognorm", sd=0.025, n=40, seed=7)
+
+
+@pytest.mark.parametrize("zoom", [0.5, 1.5, 2.0, 3.0])
+def test_pixelwise_zoom(cuda, fgl, orc, zoom):
+    _check("pixel", fgl, orc, _blobs(40, 36), radius=0.1, n=16, zoom=zoom, seed=9)
+
+
+def test_pixelwise_cell_and_absolute_max_radius(cuda, fgl, orc):
+    _check("pixel", fgl, orc, _blobs(40, 40), radius=0.15, n=20, cell=0.37, maxr=0.3, seed=13)
+
+
+def test_pixelwise_rejection_regime(cuda, fgl, orc):
+    """cell 1.0, radius 0.2: lambda*delta^2 >= 12 in bright areas (Poisson rejection branch)."""
+    plane = np.clip(workloads.ramp_noise(32, 32, 5) * 1.2, 0, 1).astype(np.float32)
+    _check("pixel", fgl, orc, plane, radius=0.2, n=16, cell=1.0, seed=17)
+
+
+def test_pixelwise_dense_subdivides(cuda, fgl, orc):
+    """A saturated plane: every window overflows shared memory and splits into quadrants."""
+    plane = np.ones((24, 24), np.float32)
+    _check("pixel", fgl, orc, plane, radius=0.05, n=12, seed=19)
+    _, _, subdiv, _ = fgl.pixelwise_diagnostics()
+    assert subdiv > 0
+
+
+def test_pixelwise_empty_and_tiny(cuda, fgl, orc):
+    _check("pixel", fgl, orc, np.zeros((16, 16), np.float32), radius=0.1, n=8)
+    _check("pixel", fgl, orc, np.full((1, 1), 0.5, np.float32), radius=0.1, n=8)
+    _check("pixel", fgl, orc, np.full((2, 3), 0.7, np.float32), radius=0.3, n=5, zoom=2.0)
+
+
+def test_pixelwise_wide_filter(cuda, fgl, orc):
+    _check("pixel", fgl, orc, _blobs(32, 32), radius=0.1, n=32, sigma=4.0, seed=21)
+
+
+def test_pixelwise_forced_size(cuda, fgl, orc):
+    """--size changes the output grid while the integrator keeps mapping with params.zoom."""
+    _check("pixel", fgl, orc, _blobs(40, 30), radius=0.1, n=12, size=(50, None), seed=23)
+
+
+# ------------------------------------------------------------------ grain-wise
+def test_grainwise_blob_crop_lognormal_zoom2_n128(cuda, fgl, orc):
+    """A 96x80 crop of the 1024^2 blob workload: lognormal 0.05/0.025, zoom 2, N=128."""
+    plane = workloads.blobs_plane(1024, 1024, 0)[300:380, 400:496]
+    _check("grain", fgl, orc, np.ascontiguousarray(plane), radius=0.05, dist="lognorm", sd=0.025, zoom=2.0, n=128,
+           seed=42)
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 200])
+def test_grainwise_sample_counts(cuda, fgl, orc, n):
+    _check("grain", fgl, orc, _blobs(40, 36), radius=0.1, n=n, seed=5)
+
+
+@pytest.mark.parametrize("zoom", [0.5, 1.0, 1.5, 4.0])
+def test_grainwise_zoom(cuda, fgl, orc, zoom):
+    _check("grain", fgl, orc, _blobs(36, 30), radius=0.08, n=24, zoom=zoom, seed=29)
+
+
+def test_grainwise_large_radius(cuda, fgl, orc):
+    """radius_out > 0.5 px: the disks cover several pixel centres per offset."""
+    _check("grain", fgl, orc, _blobs(24, 24), radius=0.8, n=16, zoom=2.0, maxr=1.0, seed=31)
+
+
+def test_grainwise_empty_and_tiny(cuda, fgl, orc):
+    _check("grain", fgl, orc, np.zeros((16, 16), np.float32), radius=0.1, n=8)
+    _check("grain", fgl, orc, np.full((1, 1), 0.5, np.float32), radius=0.1, n=8)
+
+
+def test_grainwise_forced_size(cuda, fgl, orc):
+    _check("grain", fgl, orc, _blobs(40, 30), radius=0.1, n=12, size=(33, 70), seed=37)
+
+
+# ------------------------------------------------------------------ whole-image path with the fused colour epilogue
+@pytest.mark.parametrize("mode", ["luma", "rgb"])
+@pytest.mark.parametrize("algo", ["pixel", "grain"])
+def test_render_image_matches_oracle(cuda, fgl, orc, mode, algo):
+    rgb = workloads.blobs_rgb(48, 40, 3)
+    p = fgl.ParamsBuilder(radius_mean=0.1, n_samples=24, zoom=1.5, seed=77,
+                          color_mode=fgl.ColorMode.Luma if mode == "luma" else fgl.ColorMode.Rgb,
+                          algo=fgl.Algo.Pixel if algo == "pixel" else fgl.Algo.Grain).build()
+    got, stats = fgl.render_with_input_image(rgb, p)
+    op = orc.params_struct("const", 0.1, 0.0, 1.5, 0.8, 24, 77)
+    want, chosen = orc.render_image(rgb, mode, 2 if algo == "pixel" else 1, op)
+    assert stats.algorithm == (fgl.Algo.Pixel if algo == "pixel" else fgl.Algo.Grain)
+    assert got.shape == want.shape
+    assert np.array_equal(got, want), f"{np.count_nonzero(got != want)} bytes differ"
+
+
+def test_render_image_roi(cuda, fgl, orc):
+    rgb = workloads.blobs_rgb(64, 64, 4)
+    p = fgl.ParamsBuilder(radius_mean=0.1, n_samples=16, seed=5, roi=fgl.Roi(8, 4, 40, 36)).build()
+    got, stats = fgl.render_with_input_image(rgb, p)
+    op = orc.params_struct("const", 0.1, 0.0, 1.0, 0.8, 16, 5)
+    want, _ = orc.render_image(np.ascontiguousarray(rgb[4:36, 8:40]), "luma", 0, op)
+    assert stats.input_size == (32, 32)
+    assert np.array_equal(got, want)
+
+
+def test_cancel_before_launch(cuda, fgl):
+    plane = _blobs(16, 16)
+    p = fgl.ParamsBuilder(n_samples=4).build()
+    d = fgl.derive_common(p, (16, 16))
+    lam = fgl.lambda_plane(fgl.normalize_plane(plane)[0], d.inv_e_pi_r2)
+    with pytest.raises(fgl.CancelledError):
+        fgl.render_pixelwise(lam, p, d, cancel=lambda: True)
+
+
+def test_device_tensors_in_and_out(cuda, fgl, orc):
+    """torch CUDA tensors go through the same entry point without host staging."""
+    torch = cuda
+    plane = _blobs(40, 32)
+    p, d, lam, op, od, offs, offs_in = _setup(fgl, orc, plane, radius=0.1, n=16, seed=41)
+    out = fgl.render_grainwise(torch.from_numpy(lam).cuda(), p, d)
+    torch.cuda.synchronize()
+    want, _ = orc.render("grain", lam, op, od, offs)
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), want.view(np.uint32))

@@ -1,0 +1,133 @@
+"""CPU tests of the oracle: the pinned ChaCha vectors, RNG invariants and sampler statistics.
+
+The reference crate ships no golden vectors; the ChaCha block function is pinned against OpenSSL
+(tests/golden/chacha20_openssl.json, made by tests/golden/make_chacha_vectors.py), the rest is
+checked through published invariants and distribution moments.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+M64 = (1 << 64) - 1
+
+
+def test_chacha20_block_matches_openssl(orc):
+    vec = json.load(open(os.path.join(GOLDEN, "chacha20_openssl.json")))
+    assert vec["rounds"] == 20 and len(vec["cases"]) >= 30
+    for c in vec["cases"]:
+        got = orc.chacha_block(np.array(c["key"], np.uint32), c["counter"], c["stream"], 20)
+        assert np.array_equal(got, np.array(c["block"], np.uint32)), c
+
+
+def test_pcg32_seed_expansion(orc):
+    vec = json.load(open(os.path.join(GOLDEN, "chacha20_openssl.json")))
+    for k in vec["pcg32_keys"]:
+        assert np.array_equal(orc.std_key(k["seed"]), np.array(k["key"], np.uint32))
+
+
+def test_std_stream_is_chacha12_keystream(orc):
+    """StdRng output = ChaCha12 blocks 0, 1, ... read as little-endian u64 pairs."""
+    seed = 0x1234_5678_9ABC_DEF0
+    key = orc.std_key(seed)
+    stream = orc.std_stream(seed, 20)
+    words = np.concatenate([orc.chacha_block(key, b, 0, 12) for b in range(3)])
+    pairs = words[0::2].astype(np.uint64) | (words[1::2].astype(np.uint64) << np.uint64(32))
+    assert np.array_equal(stream, pairs[:20])
+
+
+def _splitmix_py(x):
+    x = (x + 0x9E3779B97F4A7C15) & M64
+    z = x
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
+    return z ^ (z >> 31)
+
+
+def _rotl(x, k):
+    return ((x << k) | (x >> (64 - k))) & M64
+
+
+def test_splitmix_and_mix3_follow_rng_rs(orc):
+    for x in (0, 1, 42, M64, 0x9E3779B97F4A7C15):
+        assert orc.splitmix64(x) == _splitmix_py(x)
+    seed, stream = 42, 0xA24B1C30BEBCCF59
+    for a, b in ((0, 0), (-1, 5), (123456, -98765), (-(2**31), 2**31 - 1)):
+        st = seed ^ stream
+        st = _splitmix_py(_rotl((st + (a & M64)) & M64, 17))
+        want = _splitmix_py(_rotl((st + (b & M64)) & M64, 41))
+        assert orc.mix3(seed, stream, a, b) == want
+
+
+def _xoshiro_py(h, n):
+    s = []
+    st = h
+    for _ in range(4):
+        st = (st + 0x9E3779B97F4A7C15) & M64
+        z = st
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
+        s.append(z ^ (z >> 31))
+    out = []
+    for _ in range(n):
+        r = (_rotl((s[0] + s[3]) & M64, 23) + s[0]) & M64
+        t = (s[1] << 17) & M64
+        s[2] ^= s[0]; s[3] ^= s[1]; s[1] ^= s[2]; s[0] ^= s[3]; s[2] ^= t
+        s[3] = _rotl(s[3], 45)
+        out.append(r)
+    return out
+
+
+def test_xoshiro256pp_stream(orc):
+    for h in (0, 7, 0xDEADBEEF, M64):
+        assert [int(v) for v in orc.small_stream(h, 16)] == _xoshiro_py(h, 16)
+
+
+def test_uniform_f32_scale_and_range(orc):
+    for lo, hi in ((0.0, 1.0), (0.0, 1.0 / 9.0), (0.0, 0.025), (-2.0, 3.0)):
+        u = orc.uniform_f32_draws(lo, hi, 99, 20000)
+        assert u.min() >= np.float32(lo) and u.max() < np.float32(hi)
+        assert abs(float(u.mean()) - (lo + hi) / 2) < 0.02 * (hi - lo)
+
+
+@pytest.mark.parametrize("lam", [0.05, 0.3, 3.8, 11.9, 12.0, 88.0, 1400.0])
+def test_poisson_moments(orc, lam):
+    n = 200000
+    d = orc.poisson_draws(lam, 1234, n)
+    assert np.all(d == np.floor(d)) and d.min() >= 0
+    se = np.sqrt(lam / n)
+    assert abs(d.mean() - lam) < 6 * se + 1e-9
+    assert abs(d.var() / lam - 1) < 0.05
+
+
+def test_normal_moments(orc):
+    z = orc.normal_draws(0.0, 1.0, 77, 1_000_000)
+    assert abs(z.mean()) < 0.006
+    assert abs(z.var() - 1) < 0.006
+    assert abs((z**4).mean() - 3) < 0.05
+    assert np.mean(np.abs(z) > 3.6541528853610088) > 0  # the tail (zero_case) is exercised
+
+
+def test_log_gamma_matches_lgamma(orc):
+    from math import lgamma
+    for x in (1.0, 2.5, 13.0, 89.0, 1401.0):
+        assert abs(orc.log_gamma(x) - lgamma(x)) < 1e-9 * max(1.0, abs(lgamma(x)))
+
+
+def test_ziggurat_tables_shape(orc):
+    x, f = orc.zig_tables()
+    assert x[1] == 3.654152885361008796 and x[256] == 0.0 and f[256] == 1.0
+    assert np.all(np.diff(x[1:]) < 0) and np.all(np.diff(f[1:]) > 0)
+
+
+def test_lambda_mean_preservation(orc):
+    """Coverage of a constant plane u is ~u: lambda = -ln(1-u)/(pi E[r^2]) (src/model.rs:252-265)."""
+    for u in (0.2, 0.6):
+        plane = np.full((24, 24), u, np.float32)
+        p = orc.params_struct("const", 0.1, 0.0, 1.0, 0.8, 32, 5)
+        d, offs, offs_in = orc.derive(p, 24, 24)
+        lam = orc.lambda_plane(orc.normalize_plane(plane)[0], d.inv_e_pi_r2)
+        out, _ = orc.render("pixel", lam, p, d, offs_in)
+        assert abs(float(out.mean()) - u) < 0.03
