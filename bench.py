@@ -1,0 +1,373 @@
+"""Benchmark of the GB300 film-grain integrators (one JSON line on rank 0).
+
+Default workload (``--workload grain_rgb_1024``): plain grain-wise, RGB, 1024x1024x3 f32 input of 16
+seeded Gaussian blobs per channel over a 0.1 background, lognormal grain radius mean 0.05 px /
+std 0.025, filter sigma 0.8, N = 128, zoom 2 (2048^2 x 3 output).  A step renders one frame (three
+planes).  Metric: MC samples/s = output pixels x channels x N per second.
+
+- ``value``: the three grain-wise launches per step on device-resident lambda planes (HBM), timed with
+  CUDA events around exactly K steps, L2 flushed (256 MiB write) before every step.
+- ``e2e``: the same frame through the public C-ABI entry point fg_render_image from pinned host f32 RGB
+  to pinned host u8 RGB (host colour split, lambda planes, H2D, kernels, fused colour, D2H).
+- ``roofline``: SM instruction issue (this path is integer/f32 ALU work: no dense contraction, almost
+  no HBM traffic).  achieved = algorithmic lane-ops per launch / the launch's CUDA-event duration; the
+  lane-op count comes from oracle-counted per-grain quantities; peak = SMs x 128 lanes
+  x the SM clock sampled during the run.
+- ``cpu_baseline``: the CPU oracle (a C restatement of the reference's integrator, OpenMP over input
+  rows as the reference's rayon loop) timed on bands of input rows of the same frame; its full-frame
+  rate is extrapolated by grain count (work is proportional to grains).
+- ``--impl reference``: that CPU oracle alone, all host threads, each step one band.
+
+Multi-GPU (torchrun): every rank renders its own frame (replicas, weak scaling); value = all ranks'
+samples / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "grain_rgb_1024": dict(desc="plain grain-wise RGB 1024x1024x3 -> 2048x2048x3, lognormal r 0.05/0.025, N 128, zoom 2",
+                           w=1024, h=1024, mode="rgb", algo="grain", radius=0.05, dist="lognorm", sd=0.025, zoom=2.0,
+                           n=128, seed=42, image_seed=0),
+    "pixel_luma_256": dict(desc="plain pixel-wise luma 256x256 ramp+noise, const r 0.12, N 64, zoom 1, seed 42",
+                           w=256, h=256, mode="luma", algo="pixel", radius=0.12, dist="const", sd=0.0, zoom=1.0, n=64,
+                           seed=42, image_seed=42),
+    "pixel_rgb_4096": dict(desc="plain pixel-wise RGB 4096x4096x3 blobs, lognormal r 0.025/0.01, N 256, zoom 1",
+                           w=4096, h=4096, mode="rgb", algo="pixel", radius=0.025, dist="lognorm", sd=0.01, zoom=1.0,
+                           n=256, seed=42, image_seed=1),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def make_input(wl):
+    from film_grain_gb300 import workloads
+    if wl["mode"] == "luma" and wl["algo"] == "pixel":
+        return workloads.gray_rgb(workloads.ramp_noise(wl["w"], wl["h"], wl["image_seed"]))
+    return workloads.blobs_rgb(wl["w"], wl["h"], wl["image_seed"])
+
+
+def build_params(fg, wl):
+    return fg.ParamsBuilder(radius_mean=wl["radius"],
+                            radius_dist=fg.RadiusDist.Lognorm if wl["dist"] == "lognorm" else fg.RadiusDist.Const,
+                            radius_stddev=wl["sd"], zoom=wl["zoom"], n_samples=wl["n"], seed=wl["seed"],
+                            color_mode=fg.ColorMode.Rgb if wl["mode"] == "rgb" else fg.ColorMode.Luma,
+                            algo=fg.Algo.Grain if wl["algo"] == "grain" else fg.Algo.Pixel).build()
+
+
+def host_planes(rgb, mode):
+    """The colour workspace planes the integrators see (load_rgb_workspace / load_luma_workspace)."""
+    c = np.clip(rgb, 0.0, 1.0).astype(np.float32)
+    if mode == "rgb":
+        return [np.ascontiguousarray(c[:, :, i]) for i in range(3)]
+    y = (np.float32(0.2126) * c[:, :, 0] + np.float32(0.7152) * c[:, :, 1]) + np.float32(0.0722) * c[:, :, 2]
+    return [np.ascontiguousarray(np.clip(y, 0.0, 1.0).astype(np.float32))]
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        self.idx = gpu_index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_grain_baseline(oracle, planes, wl, threads, band_rows=None, bands=1, count=True):
+    """Time the oracle on `bands` input-row bands per plane (4 rows per host thread, so every thread
+    of the row-parallel loop is busy); extrapolate to the frame by grain count.
+    Returns (samples_per_s, seconds_measured, sample description, per-plane work counts)."""
+    band_rows = band_rows or 4 * threads
+    p = oracle.params_struct(wl["dist"], wl["radius"], wl["sd"], wl["zoom"], 0.8, wl["n"], wl["seed"])
+    h, w = planes[0].shape
+    d, offs, _ = oracle.derive(p, w, h)
+    frame_samples = d.out_w * d.out_h * len(planes) * wl["n"]
+    t_frame, t_meas, counts = 0.0, 0.0, []
+    bits = np.zeros(d.out_w * d.out_h * ((wl["n"] + 63) // 64), np.uint64)
+    for ci, plane in enumerate(planes):
+        lam = oracle.lambda_plane(oracle.normalize_plane(plane)[0], d.inv_e_pi_r2)
+        g_full = oracle.grain_total(lam, p, d, threads=threads)
+        g_band, t_band, st_tot = 0, 0.0, np.zeros(4, np.uint64)
+        for b in range(bands):
+            y0 = int((b + 0.5) * h / bands) - band_rows // 2
+            if count:
+                st, _ = oracle.grainwise_rows(lam, p, d, offs, (y0, y0 + band_rows), count=True, threads=threads,
+                                              bits=bits)
+                st_tot += st
+            t0 = time.perf_counter()
+            st, _ = oracle.grainwise_rows(lam, p, d, offs, (y0, y0 + band_rows), count=False, threads=threads,
+                                          bits=bits)
+            t_band += time.perf_counter() - t0
+            g_band += int(st[0])
+        t_meas += t_band
+        t_frame += t_band * g_full / max(1, g_band)
+        gb = max(1, int(st_tot[0]))
+        counts.append(dict(grains=g_full, px_per_grain=float(st_tot[1]) / gb, py_per_grain=float(st_tot[2]) / gb,
+                           hits_per_grain=float(st_tot[3]) / gb))
+    desc = (f"{bands} bands x {band_rows} input rows per plane ({len(planes)} planes) through the reference's full "
+            f"grain-wise loop; frame time extrapolated by grain count")
+    return frame_samples / t_frame, t_meas, desc, counts
+
+
+def cpu_pixel_baseline(oracle, planes, wl, threads, rows=None):
+    p = oracle.params_struct(wl["dist"], wl["radius"], wl["sd"], wl["zoom"], 0.8, wl["n"], wl["seed"])
+    h, w = planes[0].shape
+    d, offs, offs_in = oracle.derive(p, w, h)
+    lam = oracle.lambda_plane(oracle.normalize_plane(planes[0])[0], d.inv_e_pi_r2)
+    r = rows or d.out_h
+    y0 = max(0, d.out_h // 2 - r // 2)
+    t0 = time.perf_counter()
+    oracle.render("pixel", lam, p, d, offs_in, rect=(0, y0, d.out_w, y0 + r), threads=threads)
+    dt = time.perf_counter() - t0
+    samples = d.out_w * r * wl["n"]
+    return samples / dt, dt, f"output rows {y0}..{y0 + r} of plane 0 ({samples} samples)", None
+
+
+# Algorithmic lane-ops of the grain-wise path (minimal exact implementation; derivation in the design doc).
+GW_COST = dict(grain_lognorm=150, grain_const=70, x_pair=10, y_pair=8, hit=12, out_base=3, out_word=2)
+
+
+def grainwise_lane_ops(count, wl, out_px):
+    words = (wl["n"] + 31) // 32
+    g = count["grains"]
+    per_grain = GW_COST["grain_lognorm"] if wl["dist"] == "lognorm" else GW_COST["grain_const"]
+    return (g * (per_grain + GW_COST["x_pair"] * count["px_per_grain"] + GW_COST["y_pair"] * count["py_per_grain"] +
+                 GW_COST["hit"] * count["hits_per_grain"]) + out_px * (GW_COST["out_base"] + GW_COST["out_word"] * words))
+
+
+def run_reference(args, wl, rank):
+    import oracle
+    if rank != 0:
+        return
+    oracle.build()
+    threads = os.cpu_count() or 1
+    rgb = make_input(wl)
+    planes = host_planes(rgb, wl["mode"])
+    vals = []
+    desc = ""
+    for i in range(args.warmup + args.steps):
+        if wl["algo"] == "grain":
+            v, _, desc, _ = cpu_grain_baseline(oracle, planes, wl, threads, count=False)
+        else:
+            v, _, desc, _ = cpu_pixel_baseline(oracle, planes, wl, threads, rows=None if wl["w"] <= 256 else 16)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": "MC samples/s", "value": value, "unit": "samples/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64-rng/f32", "data": "synthetic (seeded)",
+            "config": {"workload": args.workload, "description": wl["desc"]},
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
+                             "sample": desc + "; each step one sample"},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="grain_rgb_1024", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    wl = WORKLOADS[args.workload]
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, wl, rank)
+        return
+
+    import torch
+    import film_grain_gb300 as fg
+    from film_grain_gb300 import build as fgbuild
+    fgbuild.build()
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    L = fg.lib()
+    rgb = make_input(wl)
+    params = build_params(fg, wl)
+    derived = fg.derive_common(params, (wl["w"], wl["h"]))
+    planes = host_planes(rgb, wl["mode"])
+    lam_host = [fg.lambda_plane(fg.normalize_plane(pl)[0], derived.inv_e_pi_r2) for pl in planes]
+    lam_dev = [torch.from_numpy(l).cuda() for l in lam_host]
+    ow, oh = derived.output_width, derived.output_height
+    outs = [torch.empty((oh, ow), dtype=torch.float32, device="cuda") for _ in planes]
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    offs = np.ascontiguousarray(derived.offsets if wl["algo"] == "grain" else derived.offsets_input, np.float32)
+    fn = L.fg_render_grainwise_async if wl["algo"] == "grain" else L.fg_render_pixelwise_async
+    launches_per_plane = 1 if wl["algo"] == "grain" else 3  # pixel: cell table, tile kernel, epilogue
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    ev = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in planes] for _ in range(args.steps)]
+
+    def step(i=None):
+        flush.fill_(1.0)
+        for c in range(len(planes)):
+            if i is not None:
+                ev[i][c][0].record(stream)
+            rc = fn(lam_dev[c].data_ptr(), params.c, derived._c, offs.ctypes.data, outs[c].data_ptr(), sp)
+            if rc != 0:
+                raise RuntimeError(L.fg_last_error_message().decode())
+            if i is not None:
+                ev[i][c][1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    if clocks:
+        clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    launch_ms = []
+    t_start.record(stream)
+    for i in range(args.steps):
+        step(i)
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    for c in range(len(planes)):  # mean duration of plane c's launch over the timed steps
+        launch_ms.append(sum(ev[i][c][0].elapsed_time(ev[i][c][1]) for i in range(args.steps)) / args.steps)
+    elapsed = t_start.elapsed_time(t_end) / 1e3
+    if dist:
+        dist.barrier()
+        tt = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        elapsed = float(tt.item())
+    clk = clocks.stop() if clocks else None
+
+    samples_per_frame = ow * oh * len(planes) * wl["n"]
+    value = samples_per_frame * args.steps * world / elapsed
+    ms_per_step = elapsed / args.steps * 1e3
+
+    # ---- end to end through the public entry point, pinned host buffers
+    pin_in = torch.from_numpy(rgb).pin_memory()
+    pin_out = torch.empty((oh, ow, 3), dtype=torch.uint8).pin_memory()
+    st = fg._StatsC()
+    e2e_fn = lambda: L.fg_render_image(pin_in.data_ptr(), wl["w"], wl["h"], ctypes.byref(params.c), pin_out.data_ptr(),
+                                       ctypes.byref(st), None, sp)
+    for _ in range(args.warmup):
+        assert e2e_fn() == 0, L.fg_last_error_message()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        assert e2e_fn() == 0
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    h2d = 4 * wl["w"] * wl["h"] * len(planes) + (16 if wl["algo"] == "grain" else 8) * wl["n"]
+    if wl["mode"] == "luma":
+        h2d += 8 * wl["w"] * wl["h"]
+    d2h = 3 * ow * oh
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    line = {"metric": "MC samples/s", "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64-rng/f32", "data": "synthetic (seeded, generated in bench.py)",
+            "config": {"workload": args.workload, "description": wl["desc"], "frame_samples": samples_per_frame,
+                       "ms_per_frame": ms_per_step, "l2": "256 MiB flush write before every step",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": samples_per_frame / e2e_s, "unit": "samples/s", "ms_per_frame": e2e_s * 1e3,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "path": "fg_render_image: pinned f32 RGB in -> pinned u8 RGB out"},
+            "gpu_launches": args.steps * len(planes) * launches_per_plane,
+            "clocks": clk}
+
+    # ---- roofline of the dominant kernel and the CPU baseline
+    sm_count = torch.cuda.get_device_properties(0).multi_processor_count
+    f_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    peak = sm_count * 128 * f_mhz * 1e6  # lane-ops/s
+    counts = None
+    if not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        threads = os.cpu_count() or 1
+        if wl["algo"] == "grain":
+            cpu_v, cpu_t, desc, counts = cpu_grain_baseline(oracle, planes, wl, threads)
+        else:
+            cpu_v, cpu_t, desc, _ = cpu_pixel_baseline(oracle, planes, wl, threads,
+                                                        rows=None if wl["w"] <= 256 else 8)
+        line["cpu_baseline"] = {"value": cpu_v, "unit": "samples/s", "cores": threads, "kind": "port",
+                                "sample": desc, "seconds": cpu_t}
+    if counts and wl["algo"] == "grain":
+        ops = [grainwise_lane_ops(c, wl, ow * oh) for c in counts]
+        ach = sum(o / (ms / 1e3) for o, ms in zip(ops, launch_ms)) / len(ops)
+        line["roofline"] = {"bound": "sm_issue", "achieved": ach / 1e12, "peak": peak / 1e12, "unit": "Tlane-op/s",
+                            "frac": ach / peak, "traffic": None,
+                            "kernel": "grainwise_kernel", "launch_ms": launch_ms,
+                            "lane_ops_per_launch": ops, "counts": counts,
+                            "peak_basis": f"{sm_count} SMs x 128 lanes x {f_mhz:.0f} MHz (sampled)"}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

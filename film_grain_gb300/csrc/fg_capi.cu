@@ -130,14 +130,29 @@ fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_der
     return FG_OK;
 }
 
+void sorted_offset_table(const float *h_offs, uint32_t n, float4 *table) {
+    std::vector<float4> t(n);
+    for (uint32_t k = 0; k < n; k++) {
+        float ox = h_offs[2 * k], oy = h_offs[2 * k + 1];
+        float fx = ox - std::floor(ox);
+        if (!(fx < 1.0f)) fx = 0.0f;  // a tiny negative offset can round up to 1; cyclically that is 0
+        int kb = (int)k;
+        float kf;
+        std::memcpy(&kf, &kb, 4);
+        t[k] = make_float4(fx, ox, oy, kf);
+    }
+    std::stable_sort(t.begin(), t.end(), [](const float4 &a, const float4 &b) { return a.x < b.x; });
+    std::copy(t.begin(), t.end(), table);
+}
+
 GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const float *h_offs, const float *d_lam,
-                             const float *d_offs, float *d_out) {
+                             const float4 *d_table, float *d_out) {
     GrainwiseArgs a;
     std::memset(&a, 0, sizeof a);
     float ext[4];
     offset_extents(h_offs, p.n_samples, ext);
     a.lam = d_lam;
-    a.offs = reinterpret_cast<const float2 *>(d_offs);
+    a.sorted_offs = d_table;
     a.out = d_out;
     a.in_w = (int)d.input_width; a.in_h = (int)d.input_height;
     a.out_w = (int)d.output_width; a.out_h = (int)d.output_height;
@@ -151,6 +166,13 @@ GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const floa
     a.rm = d.rm;
     a.zoom = p.zoom;
     a.offx_min = ext[0]; a.offx_max = ext[1]; a.offy_min = ext[2]; a.offy_max = ext[3];
+    // Rounding margin of the candidate interval: each of the three f32 roundings between
+    // czx + offx and the bounds() comparison moves a value by at most half an ulp of the largest
+    // coordinate M; the fraction arithmetic adds a few 2^-24.
+    const double M = (double)std::max(d.output_width, d.output_height) + 8.0 +
+                     std::max(std::max(-ext[0], ext[1]), std::max(-ext[2], ext[3])) + d.rm * p.zoom;
+    const double U = std::ldexp(1.0, (int)std::floor(std::log2(M)) - 23);
+    a.frac_eps = (float)(4.0 * U + std::ldexp(1.0, -20));
     a.seed = p.seed;
     a.lognorm = p.radius_dist == FG_RADIUS_LOGNORM;
     a.radius_mean = p.radius_mean;
@@ -160,7 +182,7 @@ GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const floa
 }
 
 fg_status enqueue_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
-    if ((size_t)a.n * sizeof(float2) + (size_t)a.tile_w * a.tile_h * a.words * 4 > 200 * 1024)
+    if (grainwise_smem_bytes(a) > 200 * 1024)
         return set_error(FG_ERR_UNSUPPORTED, "n_samples too large for the grain-wise tile");
     FG_CUDA(launch_grainwise(a, s), "grainwise kernel");
     return FG_OK;
@@ -225,7 +247,14 @@ static fg_status render_plane_sync(int algo, const float *lambda, const fg_param
         FG_CUDA(b_out.alloc(sizeof(float) * n_out, s), "alloc out");
         d_out = (float *)b_out.p;
     }
-    if (!offs_dev) {
+    if (algo == FG_ALGO_GRAIN) {
+        std::vector<float4> tab(p.n_samples);
+        sorted_offset_table(h_offs.data(), p.n_samples, tab.data());
+        FG_CUDA(b_offs.alloc(sizeof(float4) * p.n_samples, s), "alloc offsets");
+        FG_CUDA(cudaMemcpyAsync(b_offs.p, tab.data(), sizeof(float4) * p.n_samples, cudaMemcpyHostToDevice, s),
+                "offsets H2D");
+        d_offs = (const float *)b_offs.p;
+    } else if (!offs_dev) {
         FG_CUDA(b_offs.alloc(off_bytes, s), "alloc offsets");
         FG_CUDA(cudaMemcpyAsync(b_offs.p, h_offs.data(), off_bytes, cudaMemcpyHostToDevice, s), "offsets H2D");
         d_offs = (const float *)b_offs.p;
@@ -237,7 +266,7 @@ static fg_status render_plane_sync(int algo, const float *lambda, const fg_param
         st = enqueue_pixelwise(d_lam, p, d, h_offs.data(), d_offs, d_out, (CellParam *)b_cells.p,
                                (unsigned long long *)b_diag.p, nullptr, s);
     } else {
-        GrainwiseArgs a = grainwise_args(p, d, h_offs.data(), d_lam, d_offs, d_out);
+        GrainwiseArgs a = grainwise_args(p, d, h_offs.data(), d_lam, (const float4 *)d_offs, d_out);
         st = enqueue_grainwise(a, s);
     }
     if (st != FG_OK) {
@@ -298,11 +327,13 @@ FG_API fg_status fg_render_grainwise_async(const float *d_lambda, const fg_param
     if (is_device_ptr(offsets)) return set_error(FG_ERR_INVALID, "offsets must be host memory");
     keep_pool_memory();
     cudaStream_t s = (cudaStream_t)stream;
-    const size_t off_bytes = sizeof(float) * 2 * params->n_samples;
+    std::vector<float4> tab(params->n_samples);
+    sorted_offset_table(offsets, params->n_samples, tab.data());
     DevBuf b_offs;
-    FG_CUDA(b_offs.alloc(off_bytes, s), "alloc offsets");
-    FG_CUDA(cudaMemcpyAsync(b_offs.p, offsets, off_bytes, cudaMemcpyHostToDevice, s), "offsets H2D");
-    GrainwiseArgs a = grainwise_args(*params, *derived, offsets, d_lambda, (const float *)b_offs.p, d_out);
+    FG_CUDA(b_offs.alloc(sizeof(float4) * params->n_samples, s), "alloc offsets");
+    FG_CUDA(cudaMemcpyAsync(b_offs.p, tab.data(), sizeof(float4) * params->n_samples, cudaMemcpyHostToDevice, s),
+            "offsets H2D");
+    GrainwiseArgs a = grainwise_args(*params, *derived, offsets, d_lambda, (const float4 *)b_offs.p, d_out);
     return enqueue_grainwise(a, s);
 }
 
@@ -343,10 +374,18 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
     FG_CUDA(b_lam.alloc(sizeof(float) * n_in * nplanes, s), "alloc lambda");
     FG_CUDA(b_out.alloc(sizeof(float) * n_out * nplanes, s), "alloc planes");
     FG_CUDA(b_rgb8.alloc(3 * n_out, s), "alloc rgb8");
-    FG_CUDA(b_offs.alloc(sizeof(float) * 2 * p.n_samples, s), "alloc offsets");
-    const float *h_offs_used = algo == FG_ALGO_PIXEL ? offs_in.data() : offs.data();
-    FG_CUDA(cudaMemcpyAsync(b_offs.p, h_offs_used, sizeof(float) * 2 * p.n_samples, cudaMemcpyHostToDevice, s),
-            "offsets H2D");
+    std::vector<float4> tab;
+    if (algo == FG_ALGO_PIXEL) {
+        FG_CUDA(b_offs.alloc(sizeof(float) * 2 * p.n_samples, s), "alloc offsets");
+        FG_CUDA(cudaMemcpyAsync(b_offs.p, offs_in.data(), sizeof(float) * 2 * p.n_samples, cudaMemcpyHostToDevice, s),
+                "offsets H2D");
+    } else {
+        tab.resize(p.n_samples);
+        sorted_offset_table(offs.data(), p.n_samples, tab.data());
+        FG_CUDA(b_offs.alloc(sizeof(float4) * p.n_samples, s), "alloc offsets");
+        FG_CUDA(cudaMemcpyAsync(b_offs.p, tab.data(), sizeof(float4) * p.n_samples, cudaMemcpyHostToDevice, s),
+                "offsets H2D");
+    }
     float *d_lam = (float *)b_lam.p, *d_out = (float *)b_out.p;
     float *d_cb = nullptr, *d_cr = nullptr;
     if (luma) {
@@ -384,7 +423,7 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
             st = enqueue_pixelwise(d_lam + (size_t)c * n_in, p, d, offs_in.data(), (const float *)b_offs.p, d_plane,
                                    (CellParam *)b_cells.p, (unsigned long long *)b_diag.p, &e, s);
         } else {
-            GrainwiseArgs a = grainwise_args(p, d, offs.data(), d_lam + (size_t)c * n_in, (const float *)b_offs.p,
+            GrainwiseArgs a = grainwise_args(p, d, offs.data(), d_lam + (size_t)c * n_in, (const float4 *)b_offs.p,
                                              d_plane);
             if (luma) {
                 a.out_rgb8 = (unsigned char *)b_rgb8.p;

@@ -3,96 +3,297 @@
 // The reference walks input pixels, draws Poisson(lambda) grains from each pixel's stream, and for
 // every grain and offset k ORs bit k into the 64-bit sample masks of the output pixels whose centres
 // fall in the offset disk (AtomicU64::fetch_or), then popcounts the masks.  Here one CTA owns an
-// output tile: its N-bit masks live in shared memory as ceil(N/32) 32-bit words per pixel; the CTA
-// regenerates the grains of every input pixel whose offset disks can reach the tile (the pixel
-// streams are deterministic, so tiles never need each other's grains), rasterises them with the
-// reference's exact bounds() and centre test, and finishes with the popcount * (1/N) epilogue --
-// optionally fused with the luma colour recombination and u8 packing.  Bits are set with
-// shared-memory atomicOr; OR is idempotent and commutative, so the result is independent of order.
+// output tile and keeps its N-bit masks in shared memory (ceil(N/32) words per pixel).  It
+// regenerates the grains of every input pixel whose offset disks can reach the tile (pixel streams
+// are deterministic, so tiles never exchange grains), rasterises them with the reference's exact
+// bounds() and centre test, and finishes with the popcount * (1/N) epilogue -- optionally fused
+// with the luma colour recombination and u8 packing.
+//
+// Work organisation:
+//   - each warp takes 32 footprint pixels at a time (one per lane, Poisson set-up in step) and
+//     draws their grains one per lane per step; valid grains are compacted into a 64-entry warp
+//     queue with a ballot, and every full batch of 32 is rasterised grain by grain by the whole warp;
+//   - the offsets are sorted by the fractional part of their x component.  An offset can put a
+//     pixel centre inside a grain's disk only if frac(czx + offx) lies within radius_out of 1/2, so
+//     only the cyclic interval of the sorted table around frac(1/2 - czx), widened by a rounding
+//     margin, is scanned -- the lanes stride over it, each entry still going through the exact
+//     reference test;
+//   - the lognormal radius is evaluated with the double-float exp (exp_f64_to_f32).
+// Bits are set with shared-memory atomicOr; OR is idempotent and commutative, so the result does not
+// depend on the order.
 #include "fg_kernels.cuh"
 #include "fg_rng.cuh"
 #include "fg_color.cuh"
 
 namespace fg {
 
-constexpr int kGwThreads = 256;
+constexpr int kGwThreads = 512;
+constexpr int kGwWarps = kGwThreads / 32;
+constexpr int kGwQueue = 64;     // grains per warp queue (a full batch of 32 plus a partial step)
+constexpr int kGwPairs = 64;     // surviving (grain, offset) pairs per warp queue
+constexpr int kGwBuckets = 256;  // bucket index over the sorted offset fractions
 
-__device__ __forceinline__ int gw_f2i(float v) { return __float2int_rz(v); }
+struct GwTile {
+    int tx0, ty0, tile_w, words;
+    float ftx0, fty0, ftx1m, fty1m;  // tile bounds as floats: first and last column / row
+};
 
-__global__ void __launch_bounds__(kGwThreads) grainwise_kernel(const GrainwiseArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2 *offs = reinterpret_cast<float2 *>(smem_raw);
-    unsigned int *mask = reinterpret_cast<unsigned int *>(offs + a.n);
-    const int tid = threadIdx.x;
-    const int tx0 = blockIdx.x * a.tile_w, ty0 = blockIdx.y * a.tile_h;
-    const int tx1 = min(tx0 + a.tile_w, a.out_w), ty1 = min(ty0 + a.tile_h, a.out_h);
-    const int words = a.words;
-    const int tile_words = a.tile_w * a.tile_h * words;
+// floor / ceil of an f32.  With kSmall (every coordinate within +-2^22) they are one directed-rounding
+// add and one exact subtract of 1.5 * 2^23, which stay on the FP32 pipes.
+template <bool kSmall>
+__device__ __forceinline__ float gw_floor(float v) {
+    if (kSmall) return __fsub_rn(__fadd_rd(v, 12582912.0f), 12582912.0f);
+    return floorf(v);
+}
+template <bool kSmall>
+__device__ __forceinline__ float gw_ceil(float v) {
+    if (kSmall) return __fsub_rn(__fadd_ru(v, 12582912.0f), 12582912.0f);
+    return ceilf(v);
+}
 
-    for (int k = tid; k < a.n; k += kGwThreads) offs[k] = a.offs[k];
-    for (int t = tid; t < tile_words; t += kGwThreads) mask[t] = 0u;
-    __syncthreads();
+// bounds(center, radius, limit) (src/grainwise.rs:126-142) intersected with the tile's rows or
+// columns [lo_t, hi_t] (a subset of [0, limit-1]): with lo = ceil((c - r) - 0.5) and
+// hi = floor((c + r) - 0.5), the reference yields Some iff lo <= hi, lo <= limit-1 and hi >= 0, and
+// then clamps to [0, limit-1]; intersecting that with [lo_t, hi_t] leaves [max(lo, lo_t),
+// min(hi, hi_t)], which is empty exactly when one of the reference's conditions fails or the range
+// misses the tile.  Coordinates stay below 2^24, so comparing integral floats is the reference's i32
+// comparison.
+template <bool kSmall>
+__device__ __forceinline__ bool gw_range(float c, float r, float lo_t, float hi_t, float &a, float &b) {
+    a = fmaxf(gw_ceil<kSmall>(FG_FSUB(FG_FSUB(c, r), 0.5f)), lo_t);
+    b = fminf(gw_floor<kSmall>(FG_FSUB(FG_FADD(c, r), 0.5f)), hi_t);
+    return a <= b;
+}
 
-    // Input pixels whose grains can reach the tile (conservative: one extra pixel of margin).
-    const float reach = FG_FMUL(a.rm, a.zoom) + 2.0f;
-    const int ix0 = max(0, (int)floorf(((float)tx0 - reach - a.offx_max) / a.zoom) - 1);
-    const int ix1 = min(a.in_w, (int)ceilf(((float)tx1 + reach - a.offx_min) / a.zoom) + 1);
-    const int iy0 = max(0, (int)floorf(((float)ty0 - reach - a.offy_max) / a.zoom) - 1);
-    const int iy1 = min(a.in_h, (int)ceilf(((float)ty1 + reach - a.offy_min) / a.zoom) + 1);
-    const int fw = ix1 - ix0, fh = iy1 - iy0;
-    const UniformF32 U = uniform_f32_new(0.0f, 1.0f);
-    const float zoom = a.zoom;
-    const int last_x = a.out_w - 1, last_y = a.out_h - 1;
+// Stage B: the reference's centre tests and bit sets of one surviving (grain, offset) pair
+// (src/grainwise.rs:80-101), restricted to the tile.  P = (tx, ty, radius_out, k).
+template <bool kSmall>
+__device__ __forceinline__ void gw_splat(const GwTile &T, unsigned int *mask, const float4 P) {
+    const float tx = P.x, ty = P.y, ro = P.z;
+    const int k = __float_as_int(P.w);
+    const float rsq = FG_FMUL(ro, ro);
+    float y0, y1, x0, x1;
+    if (!gw_range<kSmall>(ty, ro, T.fty0, T.fty1m, y0, y1)) return;
+    if (!gw_range<kSmall>(tx, ro, T.ftx0, T.ftx1m, x0, x1)) return;
+    const unsigned bit = 1u << (k & 31);
+    unsigned int *base = mask + (k >> 5);
+    int row = (int)(y0 - T.fty0) * T.tile_w;
+    for (float oy = y0; oy <= y1; oy = FG_FADD(oy, 1.0f), row += T.tile_w) {
+        const float dy = FG_FSUB(FG_FADD(oy, 0.5f), ty);
+        const float dysq = FG_FMUL(dy, dy);
+        if (dysq > rsq) continue;
+        int col = (int)(x0 - T.ftx0);
+        for (float ox = x0; ox <= x1; ox = FG_FADD(ox, 1.0f), col++) {
+            const float dx = FG_FSUB(FG_FADD(ox, 0.5f), tx);
+            if (FG_FADD(FG_FMUL(dx, dx), dysq) <= rsq) atomicOr(base + (row + col) * T.words, bit);
+        }
+    }
+}
 
-    if (fw > 0 && fh > 0) {
-        for (int p = tid; p < fw * fh; p += kGwThreads) {
-            const int x = ix0 + p % fw, y = iy0 + p / fw;
-            const float lv = a.lam[(long long)y * a.in_w + x];
-            if (!(lv > 0.0f)) continue;
-            Xoshiro rng = pixel_rng(a.seed, x, y);
-            const PoissonParams P = poisson_new((double)lv);
-            const uint32_t q = poisson_sample(P, rng);
-            for (uint32_t g = 0; g < q; g++) {
-                const float cx = FG_FADD((float)x, uniform_f32_from(U, rng.next()));
-                const float cy = FG_FADD((float)y, uniform_f32_from(U, rng.next()));
-                float r = a.lognorm ? (float)exp(normal_sample(a.log_mu, a.log_sigma, rng)) : a.radius_mean;
-                if (r > a.rm) r = a.rm;
-                if (r <= 0.0f) continue;
-                const float ro = FG_FMUL(r, zoom);
-                if (ro <= 0.0f) continue;
-                const float rsq = FG_FMUL(ro, ro);
-                const float czx = FG_FMUL(cx, zoom), czy = FG_FMUL(cy, zoom);
-                for (int k = 0; k < a.n; k++) {
-                    const float2 o = offs[k];
-                    const float tx = FG_FADD(czx, o.x);
-                    const float ty = FG_FADD(czy, o.y);
-                    // bounds(tx, radius_out, output_width) (src/grainwise.rs:126-142)
-                    int xlo = gw_f2i(ceilf(FG_FSUB(FG_FSUB(tx, ro), 0.5f)));
-                    int xhi = gw_f2i(floorf(FG_FSUB(FG_FADD(tx, ro), 0.5f)));
-                    if (xhi < xlo || xlo > last_x || xhi < 0) continue;
-                    int ylo = gw_f2i(ceilf(FG_FSUB(FG_FSUB(ty, ro), 0.5f)));
-                    int yhi = gw_f2i(floorf(FG_FSUB(FG_FADD(ty, ro), 0.5f)));
-                    if (yhi < ylo || ylo > last_y || yhi < 0) continue;
-                    // clamp to the image, then keep the tile's part
-                    xlo = max(max(xlo, 0), tx0); xhi = min(min(xhi, last_x), tx1 - 1);
-                    ylo = max(max(ylo, 0), ty0); yhi = min(min(yhi, last_y), ty1 - 1);
-                    if (xlo > xhi || ylo > yhi) continue;
-                    const unsigned bit = 1u << (k & 31);
-                    const int word = k >> 5;
-                    for (int oy = ylo; oy <= yhi; oy++) {
-                        const float dy = FG_FSUB(FG_FADD((float)oy, 0.5f), ty);
-                        const float dysq = FG_FMUL(dy, dy);
-                        if (dysq > rsq) continue;
-                        for (int ox = xlo; ox <= xhi; ox++) {
-                            const float dx = FG_FSUB(FG_FADD((float)ox, 0.5f), tx);
-                            if (FG_FADD(FG_FMUL(dx, dx), dysq) <= rsq)
-                                atomicOr(&mask[((oy - ty0) * a.tile_w + (ox - tx0)) * words + word], bit);
-                        }
-                    }
+// Candidate ranges of one grain in the sorted offset table: the entries whose frac(offx) lies in the
+// cyclic interval [c - h, c + h], c = frac(1/2 - czx), h = radius_out + margin, rounded out to whole
+// buckets of the index `bstart` (bstart[b] = first entry with frac >= b / kGwBuckets).  Entries the
+// rounding adds are harmless: every entry still goes through the exact reference test.  Packed as
+// (first | end << 16) for the two pieces of the cyclic interval.
+__device__ __forceinline__ uint2 gw_candidates(const int *bstart, int n, float czx, float ro, float eps) {
+    const float h = FG_FADD(ro, eps);
+    if (h >= 0.5f) return make_uint2((unsigned)n << 16, 0u);
+    const float fz = FG_FSUB(czx, floorf(czx));     // exact
+    float c = FG_FSUB(0.5f, fz);
+    if (c < 0.0f) c = FG_FADD(c, 1.0f);
+    const float lo = FG_FSUB(c, h), hi = FG_FADD(c, h);
+    const float nb = (float)kGwBuckets;
+    int s0, e0, s1 = 0, e1 = 0;
+    if (lo < 0.0f) {  // [0, hi] and [lo + 1, 1)
+        s0 = 0;
+        e0 = bstart[min(kGwBuckets - 1, (int)(hi * nb)) + 1];
+        s1 = bstart[min(kGwBuckets - 1, max(0, (int)(FG_FADD(lo, 1.0f) * nb)))];
+        e1 = n;
+    } else if (hi >= 1.0f) {  // [lo, 1) and [0, hi - 1]
+        s0 = bstart[min(kGwBuckets - 1, (int)(lo * nb))];
+        e0 = n;
+        e1 = bstart[min(kGwBuckets - 1, max(0, (int)(FG_FSUB(hi, 1.0f) * nb))) + 1];
+    } else {
+        s0 = bstart[min(kGwBuckets - 1, (int)(lo * nb))];
+        e0 = bstart[min(kGwBuckets - 1, (int)(hi * nb)) + 1];
+    }
+    return make_uint2((unsigned)s0 | ((unsigned)e0 << 16), (unsigned)s1 | ((unsigned)e1 << 16));
+}
+
+// Stage A over one batch of `count` queued grains: the (grain, candidate offset) pairs are flattened
+// across the lanes (every lane busy), each pair gets the exact bounds test clipped to the tile, and
+// the survivors are compacted into the warp's pair queue; full batches of 32 pairs run stage B.
+template <bool kSmall>
+__device__ __forceinline__ void gw_raster_batch(const GwTile &T, unsigned int *mask, const float4 *tab,
+                                                const float4 *q, const uint2 *qr, int count, int *cpre,
+                                                float4 *pq, int &pn, int lane) {
+    int c = 0;
+    if (lane < count) {
+        const uint2 r = qr[lane];
+        c = (int)(r.x >> 16) - (int)(r.x & 0xFFFFu) + (int)(r.y >> 16) - (int)(r.y & 0xFFFFu);
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, c, o);
+        if (lane >= o) c += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, c, 31);
+    cpre[lane + 1] = c;
+    if (lane == 0) cpre[0] = 0;
+    __syncwarp();
+    int g = 0;
+    for (int base = 0; base < total; base += 32) {
+        const int t = base + lane;
+        bool surv = false;
+        float4 P;
+        if (t < total) {
+            while (cpre[g + 1] <= t) g++;
+            const uint2 r = qr[g];
+            const int o = t - cpre[g];
+            const int n0 = (int)(r.x >> 16) - (int)(r.x & 0xFFFFu);
+            const int i = o < n0 ? (int)(r.x & 0xFFFFu) + o : (int)(r.y & 0xFFFFu) + (o - n0);
+            const float4 G = q[g];
+            const float4 e = tab[i];
+            const float ty = FG_FADD(G.y, e.z);
+            float a, b;
+            if (gw_range<kSmall>(ty, G.z, T.fty0, T.fty1m, a, b)) {
+                const float tx = FG_FADD(G.x, e.y);
+                if (gw_range<kSmall>(tx, G.z, T.ftx0, T.ftx1m, a, b)) {
+                    surv = true;
+                    P = make_float4(tx, ty, G.z, e.w);
                 }
             }
         }
+        const unsigned sb = __ballot_sync(0xffffffffu, surv);
+        if (surv) pq[pn + __popc(sb & ((1u << lane) - 1u))] = P;
+        pn += __popc(sb);
+        __syncwarp();
+        if (pn >= 32) {
+            gw_splat<kSmall>(T, mask, pq[lane]);
+            __syncwarp();
+            if (lane + 32 < pn) pq[lane] = pq[lane + 32];
+            pn -= 32;
+            __syncwarp();
+        }
     }
+}
+
+template <bool kSmall>
+__global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const GrainwiseArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4 *tab = reinterpret_cast<float4 *>(smem_raw);                   // [n] sorted offsets
+    float4 *queue = tab + a.n;                                            // [warps][kGwQueue] grains
+    float4 *pairs = queue + kGwWarps * kGwQueue;                          // [warps][kGwPairs] pairs
+    uint2 *qrange = reinterpret_cast<uint2 *>(pairs + kGwWarps * kGwPairs); // [warps][kGwQueue]
+    int *cpre = reinterpret_cast<int *>(qrange + kGwWarps * kGwQueue);    // [warps][33]
+    int *bstart = cpre + kGwWarps * 33;                                   // [kGwBuckets + 1]
+    unsigned int *mask = reinterpret_cast<unsigned int *>(bstart + kGwBuckets + 3);  // 16-B aligned
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    const int tx0 = blockIdx.x * a.tile_w, ty0 = blockIdx.y * a.tile_h;
+    const int tx1 = min(tx0 + a.tile_w, a.out_w), ty1 = min(ty0 + a.tile_h, a.out_h);
+    GwTile T;
+    T.tx0 = tx0;
+    T.ty0 = ty0;
+    T.tile_w = a.tile_w;
+    T.words = a.words;
+    T.ftx0 = (float)tx0;
+    T.fty0 = (float)ty0;
+    T.ftx1m = (float)(tx1 - 1);
+    T.fty1m = (float)(ty1 - 1);
+    const int tile_words = a.tile_w * a.tile_h * a.words;
+
+    for (int k = tid; k < a.n; k += kGwThreads) tab[k] = a.sorted_offs[k];
+    for (int t = tid; t < tile_words; t += kGwThreads) mask[t] = 0u;
+    if (tid <= kGwBuckets) {  // bucket index over the sorted fractions (read from global: tab is in flight)
+        const float v = (float)tid / (float)kGwBuckets;
+        int lo = 0, hi = a.n;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (a.sorted_offs[mid].x < v) lo = mid + 1;
+            else hi = mid;
+        }
+        bstart[tid] = tid == kGwBuckets ? a.n : lo;
+    }
+    __syncthreads();
+
+    // Input pixels whose grains can reach the tile.  A grain of input pixel x has its zoomed centre
+    // czx in [x*zoom, (x+1)*zoom]; it can set a bit of tile column ox only if
+    // |ox + 0.5 - (czx + offx)| <= radius_out + (rounding), with radius_out <= rm*zoom.  `reach`
+    // adds 1/16 px to cover the f32 roundings (a few ulps of the coordinates).
+    const float reach = FG_FMUL(a.rm, a.zoom) + 0.0625f;
+    const int ix0 = max(0, (int)floorf(((float)tx0 + 0.5f - reach - a.offx_max) / a.zoom) - 1);
+    const int ix1 = min(a.in_w, (int)floorf(((float)tx1 - 0.5f + reach - a.offx_min) / a.zoom) + 1);
+    const int iy0 = max(0, (int)floorf(((float)ty0 + 0.5f - reach - a.offy_max) / a.zoom) - 1);
+    const int iy1 = min(a.in_h, (int)floorf(((float)ty1 - 0.5f + reach - a.offy_min) / a.zoom) + 1);
+    const int fw = max(0, ix1 - ix0), total = fw * max(0, iy1 - iy0);
+    const UniformF32 U = uniform_f32_new(0.0f, 1.0f);
+    const float zoom = a.zoom;
+    float4 *q = queue + warp * kGwQueue;
+    uint2 *qr = qrange + warp * kGwQueue;
+    float4 *pq = pairs + warp * kGwPairs;
+    int *wc = cpre + warp * 33;
+
+    int qn = 0;  // warp-uniform grain-queue fill
+    int pn = 0;  // warp-uniform pair-queue fill
+    for (int base = warp * 32; base < total; base += kGwThreads) {
+        // one footprint pixel per lane, Poisson set-up in step across the warp
+        const int pi = base + lane;
+        uint32_t left = 0;
+        int px = 0, py = 0;
+        Xoshiro rng = {0, 0, 0, 0};
+        if (pi < total) {
+            px = ix0 + pi % fw;
+            py = iy0 + pi / fw;
+            const float lv = a.lam[(long long)py * a.in_w + px];
+            if (lv > 0.0f) {
+                rng = pixel_rng(a.seed, px, py);
+                const PoissonParams P = poisson_new((double)lv);
+                left = poisson_sample(P, rng);
+            }
+        }
+        while (__any_sync(0xffffffffu, left > 0)) {
+            bool valid = false;
+            float4 G;
+            uint2 R;
+            if (left > 0) {
+                left--;
+                const float cx = FG_FADD((float)px, uniform_f32_from(U, rng.next()));
+                const float cy = FG_FADD((float)py, uniform_f32_from(U, rng.next()));
+                float r = a.lognorm ? lognormal_radius_f32(a.log_mu, a.log_sigma, rng) : a.radius_mean;
+                if (r > a.rm) r = a.rm;
+                if (r > 0.0f) {
+                    const float ro = FG_FMUL(r, zoom);
+                    if (ro > 0.0f) {
+                        valid = true;
+                        G = make_float4(FG_FMUL(cx, zoom), FG_FMUL(cy, zoom), ro, 0.0f);
+                        R = gw_candidates(bstart, a.n, G.x, ro, a.frac_eps);
+                    }
+                }
+            }
+            const unsigned vb = __ballot_sync(0xffffffffu, valid);
+            if (valid) {
+                const int slot = qn + __popc(vb & ((1u << lane) - 1u));
+                q[slot] = G;
+                qr[slot] = R;
+            }
+            qn += __popc(vb);
+            __syncwarp();
+            if (qn >= 32) {
+                gw_raster_batch<kSmall>(T, mask, tab, q, qr, 32, wc, pq, pn, lane);
+                __syncwarp();
+                if (lane + 32 < qn) {
+                    q[lane] = q[lane + 32];
+                    qr[lane] = qr[lane + 32];
+                }
+                qn -= 32;
+                __syncwarp();
+            }
+        }
+    }
+    if (qn > 0) gw_raster_batch<kSmall>(T, mask, tab, q, qr, qn, wc, pq, pn, lane);
+    __syncwarp();
+    if (lane < pn) gw_splat<kSmall>(T, mask, pq[lane]);
     __syncthreads();
 
     // popcount * (1/N) (src/grainwise.rs:114-122), optionally fused with the luma recombination.
@@ -100,9 +301,9 @@ __global__ void __launch_bounds__(kGwThreads) grainwise_kernel(const GrainwiseAr
     const int tw = tx1 - tx0, th = ty1 - ty0;
     for (int t = tid; t < tw * th; t += kGwThreads) {
         const int lx = t % tw, ly = t / tw;
-        const unsigned int *m = mask + (ly * a.tile_w + lx) * words;
+        const unsigned int *m = mask + (ly * a.tile_w + lx) * a.words;
         unsigned c = 0;
-        for (int w = 0; w < words; w++) c += __popc(m[w]);
+        for (int w = 0; w < a.words; w++) c += __popc(m[w]);
         const float v = FG_FMUL((float)c, inv_samples);
         const int ox = tx0 + lx, oy = ty0 + ly;
         const long long idx = (long long)oy * a.out_w + ox;
@@ -110,11 +311,13 @@ __global__ void __launch_bounds__(kGwThreads) grainwise_kernel(const GrainwiseAr
         if (a.out_rgb8) {
             float cbv, crv;
             if (a.in_w == a.out_w && a.in_h == a.out_h) {
-                cbv = a.cb[idx]; crv = a.cr[idx];
+                cbv = a.cb[idx];
+                crv = a.cr[idx];
             } else {
                 const float sxs = FG_FDIV((float)a.in_w, (float)a.out_w), sys = FG_FDIV((float)a.in_h, (float)a.out_h);
                 const long long src = (long long)nearest_src(oy, sys, a.in_h) * a.in_w + nearest_src(ox, sxs, a.in_w);
-                cbv = a.cb[src]; crv = a.cr[src];
+                cbv = a.cb[src];
+                crv = a.cr[src];
             }
             luma_rgb8(v, cbv, crv, a.out_rgb8 + 3 * idx);
         }
@@ -122,16 +325,29 @@ __global__ void __launch_bounds__(kGwThreads) grainwise_kernel(const GrainwiseAr
 }
 
 size_t grainwise_smem_bytes(const GrainwiseArgs &a) {
-    return (size_t)a.n * sizeof(float2) + (size_t)a.tile_w * a.tile_h * a.words * sizeof(unsigned int);
+    return (size_t)a.n * sizeof(float4) + (size_t)kGwWarps * kGwQueue * sizeof(float4) +
+           (size_t)kGwWarps * kGwPairs * sizeof(float4) + (size_t)kGwWarps * kGwQueue * sizeof(uint2) +
+           ((size_t)kGwWarps * 33 + kGwBuckets + 3) * sizeof(int) +
+           (size_t)a.tile_w * a.tile_h * a.words * sizeof(unsigned int);
 }
 
 cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
-    size_t smem = grainwise_smem_bytes(a);
-    cudaError_t e = cudaFuncSetAttribute(grainwise_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+    const size_t smem = grainwise_smem_bytes(a);
     dim3 grid((a.out_w + a.tile_w - 1) / a.tile_w, (a.out_h + a.tile_h - 1) / a.tile_h);
     if (grid.x == 0 || grid.y == 0) return cudaSuccess;
-    grainwise_kernel<<<grid, kGwThreads, smem, s>>>(a);
+    // The directed-rounding floor/ceil needs every bounds() argument within +-2^22.
+    const float span = (float)max(a.out_w, a.out_h) + fmaxf(fmaxf(-a.offx_min, a.offx_max), fmaxf(-a.offy_min, a.offy_max)) +
+                       a.rm * a.zoom + 4.0f;
+    cudaError_t e;
+    if (span < 4194304.0f) {
+        e = cudaFuncSetAttribute(grainwise_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        grainwise_kernel<true><<<grid, kGwThreads, smem, s>>>(a);
+    } else {
+        e = cudaFuncSetAttribute(grainwise_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        grainwise_kernel<false><<<grid, kGwThreads, smem, s>>>(a);
+    }
     return cudaGetLastError();
 }
 

@@ -20,8 +20,10 @@ PwPlan plan_pixelwise(const fg_params &p, const fg_derived &d, const float *h_of
 fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_derived &d, const float *h_offs_in,
                             const float *d_offs_in, float *d_out, CellParam *d_cells, unsigned long long *d_diag,
                             const EpilogueArgs *colour, cudaStream_t s);
+// The grain-wise offset table: entries (frac(offx), offx, offy, k) sorted by frac(offx).
+void sorted_offset_table(const float *h_offs, uint32_t n, float4 *table);
 GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const float *h_offs, const float *d_lam,
-                             const float *d_offs, float *d_out);
+                             const float4 *d_table, float *d_out);
 fg_status enqueue_grainwise(const GrainwiseArgs &a, cudaStream_t s);
 
 }  // namespace fg

@@ -45,7 +45,7 @@ struct PixelwiseArgs {
 
 struct GrainwiseArgs {
     const float *lam;           // in_w x in_h
-    const float2 *offs;         // offsets (output pixels) [n]
+    const float4 *sorted_offs;  // [n] (frac(offx), offx, offy, k as int bits), ascending frac(offx)
     float *out;                 // out_w x out_h f32 plane (may be null when out_rgb8 is used)
     unsigned char *out_rgb8;    // fused colour output (luma mode) or null
     const float *cb, *cr;       // luma mode: chroma planes at input size
@@ -54,6 +54,7 @@ struct GrainwiseArgs {
     int tile_w, tile_h;
     float rm, zoom;
     float offx_min, offx_max, offy_min, offy_max;
+    float frac_eps;             // rounding margin of the candidate-offset interval
     unsigned long long seed;
     int lognorm;
     float radius_mean;

@@ -105,7 +105,7 @@ __device__ __forceinline__ uint32_t cell_count(unsigned long long seed, int i, i
 
 __device__ __forceinline__ float radius_draw(const PixelwiseArgs &a, Xoshiro &rng) {
     if (!a.lognorm) return a.radius_mean;
-    return (float)exp(normal_sample(a.log_mu, a.log_sigma, rng));
+    return lognormal_radius_f32(a.log_mu, a.log_sigma, rng);
 }
 
 __device__ __forceinline__ const CellParam &cell_param_at(const PixelwiseArgs &a, int i, int j) {

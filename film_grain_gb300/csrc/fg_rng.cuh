@@ -297,6 +297,117 @@ FG_HD double normal_sample(double mean, double sd, Rng &rng) {
     return FG_DADD(mean, FG_DMUL(sd, std_normal(rng)));
 }
 
+// ------------------------------------------------------------------ exp(t) rounded to f32
+// LogNormal::sample(...) as f32 (src/model.rs:141-142) is RN_f32(exp(t)) of an f64 exp.  FP64
+// throughput is a small fraction of FP32 on this part, so exp(t) is evaluated in double-float
+// arithmetic on the FP32 pipes:
+//   t = th + tm + tt exactly (three floats cut from t's 53-bit significand);
+//   r = t - k*ln2 with ln2 = L1 + L2 + L3 (L1 has 12 significant bits, so k*L1 is exact);
+//   exp(r) = T[j] * exp(s), s = r - j/64, T[j] = exp(j/64) as a float pair (exp_table.h);
+//   exp(s) = 1 + s + s^2/2 (double-float) + s^3/6 + ... + s^6/720 (float tail).
+// The double-float result carries exp(t) to about 2^-43 relative.  When it lies within 2^-40 of an
+// f32 rounding midpoint the FP64 exp decides instead; otherwise RN_f32 of the double-float value
+// equals RN_f32 of any f64 exp within 2^-50 of the true value.
+#include "exp_table.h"
+#ifndef FG_EXP_FALLBACK_HOOK
+#define FG_EXP_FALLBACK_HOOK()  // counted by the native host checker in tests/native
+#endif
+
+#ifdef __CUDACC__
+static __device__ const float2 g_exp64[49] = FG_EXP64_TABLE_INIT;
+#endif
+struct FgFloat2 { float x, y; };
+static const FgFloat2 h_exp64[49] = FG_EXP64_TABLE_INIT;
+
+FG_HD float ff_fma(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+    return __fmaf_rn(a, b, c);
+#else
+    return fmaf(a, b, c);
+#endif
+}
+FG_HD void ff_two_sum(float a, float b, float &s, float &e) {
+    s = FG_FADD(a, b);
+    float bb = FG_FSUB(s, a);
+    e = FG_FADD(FG_FSUB(a, FG_FSUB(s, bb)), FG_FSUB(b, bb));
+}
+FG_HD void ff_fast_two_sum(float a, float b, float &s, float &e) {
+    s = FG_FADD(a, b);
+    e = FG_FSUB(b, FG_FSUB(s, a));
+}
+FG_HD float pow2f(int e) { return bits_f32((uint32_t)(e + 127) << 23); }  // e in [-126, 127]
+
+FG_HD float exp_f64_to_f32(double t) {
+    const uint64_t b = f64_bits(t);
+    const uint32_t E = (uint32_t)(b >> 52) & 0x7FFu;
+    if (E < 1023u - 30u) return 1.0f;                // |t| < 2^-30: exp(t) rounds to 1
+    if (E >= 1023u + 4u) {                           // |t| >= 16, inf, nan
+        FG_EXP_FALLBACK_HOOK();
+        return (float)exp(t);
+    }
+    const uint64_t m = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;  // t = +-m * 2^(E-1075)
+    const uint32_t neg = (uint32_t)(b >> 63) << 31;
+    const int e0 = (int)E - 1075;                    // in [-82, -49]
+    const float th = bits_f32(neg | ((E - 896u) << 23) | ((uint32_t)(m >> 29) & 0x7FFFFFu));
+    const float tm = bits_f32(f32_bits((float)(uint32_t)((m >> 5) & 0xFFFFFFu) * pow2f(e0 + 5)) | neg);
+    const float tt = bits_f32(f32_bits((float)(uint32_t)(m & 31u) * pow2f(e0)) | neg);
+
+    const float L1 = 0.693115234375f, L2 = 3.1946183e-05f, L3 = 1.646595e-12f;
+    const float kf = rintf(FG_FMUL(th, 1.44269504f));
+    const float a = FG_FSUB(th, FG_FMUL(kf, L1));    // exact (Sterbenz; k*L1 exact)
+    const float p2h = FG_FMUL(kf, L2);
+    const float p2l = ff_fma(kf, L2, -p2h);
+    float sh, sl, e2;
+    ff_two_sum(a, -p2h, sh, sl);
+    ff_two_sum(sh, tm, sh, e2);
+    sl = FG_FADD(FG_FADD(sl, e2), FG_FSUB(FG_FSUB(tt, p2l), FG_FMUL(kf, L3)));
+    ff_fast_two_sum(sh, sl, sh, sl);
+
+    const float jf = rintf(FG_FMUL(sh, 64.0f));      // |j| <= 23
+    const int j = (int)jf;
+    const float s = FG_FSUB(sh, FG_FMUL(jf, 0.015625f));  // exact
+    const float q = FG_FMUL(s, s);
+    const float ql = ff_fma(s, s, -q);
+    float tail = FG_FADD(0.00833333377f, FG_FMUL(s, 0.00138888892f));
+    tail = FG_FADD(0.0416666679f, FG_FMUL(s, tail));
+    tail = FG_FADD(0.166666672f, FG_FMUL(s, tail));
+    tail = FG_FMUL(FG_FMUL(s, q), tail);             // s^3/6 + s^4/24 + s^5/120 + s^6/720
+    tail = FG_FADD(tail, FG_FMUL(s, sl));            // cross term of (s + sl)^2 / 2
+    float a1, a1l;
+    ff_two_sum(s, FG_FMUL(q, 0.5f), a1, a1l);
+    a1l = FG_FADD(a1l, FG_FADD(sl, FG_FADD(FG_FMUL(ql, 0.5f), tail)));
+    float b1, b1l;
+    ff_two_sum(1.0f, a1, b1, b1l);
+    b1l = FG_FADD(b1l, a1l);
+    ff_fast_two_sum(b1, b1l, b1, b1l);
+#ifdef __CUDA_ARCH__
+    const float2 T = g_exp64[j + 24];
+#else
+    const FgFloat2 T = h_exp64[j + 24];
+#endif
+    float yh = FG_FMUL(T.x, b1);
+    float yl = ff_fma(T.x, b1, -yh);
+    yl = FG_FADD(yl, FG_FADD(FG_FMUL(T.x, b1l), FG_FMUL(T.y, b1)));
+    ff_fast_two_sum(yh, yl, yh, yl);
+    const float P = pow2f((int)kf);                  // |k| <= 23
+    const float f = FG_FMUL(yh, P), fl = FG_FMUL(yl, P);
+    const uint32_t fb = f32_bits(f);
+    const float up = FG_FSUB(bits_f32(fb + 1u), f), dn = FG_FSUB(f, bits_f32(fb - 1u));
+    const float half = fl >= 0.0f ? FG_FMUL(0.5f, up) : FG_FMUL(0.5f, dn);
+    const float dist = fabsf(FG_FSUB(fabsf(fl), half));
+    if (!(dist > FG_FMUL(f, 9.09494702e-13f)) || !(fabsf(fl) <= half)) {  // within 2^-40 of a midpoint
+        FG_EXP_FALLBACK_HOOK();
+        return (float)exp(t);
+    }
+    return f;
+}
+
+// The lognormal radius draw: LogNormal::sample (rand_distr 0.4.3) cast to f32.
+template <class Rng>
+FG_HD float lognormal_radius_f32(double mu, double sigma, Rng &rng) {
+    return exp_f64_to_f32(normal_sample(mu, sigma, rng));
+}
+
 // ChaCha12 keystream reader (StdRng), seeded through rand_core's PCG32 seed_from_u64.
 struct ChaCha12 {
     uint32_t key[8];

@@ -91,6 +91,9 @@ def lib():
             "orc_uniform_f32_draws": (None, [f32, f32, u64, i64, f32p]),
             "orc_log_gamma": (ctypes.c_double, [ctypes.c_double]),
             "orc_threads": (i32, []),
+            "orc_grain_total": (u64, [f32p, P(OParams), P(ODerived), i64, i64, i32]),
+            "orc_grainwise_rows": (ctypes.c_int, [f32p, P(OParams), P(ODerived), f32p, i64, i64, u64p, i32, u64p,
+                                                  i32]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(_lib, name)
@@ -315,3 +318,28 @@ def log_gamma(x: float) -> float:
 
 def threads() -> int:
     return lib().orc_threads()
+
+
+# ---------------------------------------------------------------- bench support
+def grain_total(lam: np.ndarray, p: OParams, d: ODerived, rows=None, threads: int = 0) -> int:
+    lam = np.ascontiguousarray(lam, np.float32)
+    y0, y1 = rows if rows else (0, d.in_h)
+    return int(lib().orc_grain_total(_p(lam, ctypes.c_float), ctypes.byref(p), ctypes.byref(d), y0, y1, threads))
+
+
+def grainwise_rows(lam: np.ndarray, p: OParams, d: ODerived, offs: np.ndarray, rows, count: bool = False,
+                   threads: int = 0, bits: np.ndarray = None):
+    """The reference's grain-wise work for input rows [y0, y1) over the whole output plane.
+    Returns (stats[4] = grains, x-bounds pairs, x-and-y-bounds pairs, bits set; bit planes)."""
+    lam = np.ascontiguousarray(lam, np.float32)
+    offs = np.ascontiguousarray(offs, np.float32)
+    lanes = (p.n_samples + 63) // 64
+    if bits is None:
+        bits = np.zeros(d.out_w * d.out_h * lanes, np.uint64)
+    else:
+        bits[:] = 0
+    stats = np.zeros(4, np.uint64)
+    lib().orc_grainwise_rows(_p(lam, ctypes.c_float), ctypes.byref(p), ctypes.byref(d), _p(offs, ctypes.c_float),
+                             rows[0], rows[1], _p(bits, ctypes.c_uint64), 1 if count else 0, _p(stats, ctypes.c_uint64),
+                             threads)
+    return stats, bits

@@ -774,3 +774,90 @@ ORC_EXPORT int32_t orc_threads(void) {
     return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------ bench support (grain-wise work accounting) */
+/* Sum of the Poisson grain counts of input rows [iy0, iy1) (the draw of src/grainwise.rs:41-43). */
+ORC_EXPORT uint64_t orc_grain_total(const float *lam, const o_params *p, const o_derived *d, int64_t iy0, int64_t iy1,
+                                    int32_t threads) {
+    uint64_t total = 0;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
+    for (int64_t y = iy0; y < iy1; y++) {
+        for (int64_t x = 0; x < d->in_w; x++) {
+            float lv = lam[y * d->in_w + x];
+            if (lv <= 0.0f) continue;
+            o_small_rng rng = o_pixel_rng(p->seed, (int32_t)x, (int32_t)y);
+            o_poisson P = o_poisson_new((double)lv);
+            total += o_f64_to_u32(o_poisson_sample(&P, o_small_next_v, &rng));
+        }
+    }
+    return total;
+}
+
+/* The reference's grain-wise work for input rows [iy0, iy1) over the whole output plane, exactly as
+ * src/grainwise.rs:29-107 does it (rayon's decomposition: rows of the input).  bits: out_w*out_h*lanes
+ * u64, zeroed by the caller.  With count != 0 it also tallies, over all (grain, offset) pairs,
+ * stats[0] grains, [1] pairs whose x bounds are Some, [2] pairs whose x and y bounds are Some,
+ * [3] centre tests passed (bits set). */
+ORC_EXPORT int orc_grainwise_rows(const float *lam, const o_params *p, const o_derived *d, const float *offsets,
+                                  int64_t iy0, int64_t iy1, uint64_t *bits, int32_t count, uint64_t stats[4],
+                                  int32_t threads) {
+    o_zig_init();
+    uint32_t n = p->n_samples;
+    int64_t out_w = d->out_w, out_h = d->out_h;
+    int64_t lanes = ((int64_t)n + 63) / 64;
+    float zoom = p->zoom;
+    uint64_t g_tot = 0, px_tot = 0, py_tot = 0, h_tot = 0;
+    o_uniform_f32 uni = o_uniform_new(0.0f, 1.0f);
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : g_tot, px_tot, py_tot, h_tot)
+    for (int64_t y = iy0; y < iy1; y++) {
+        for (int64_t x = 0; x < d->in_w; x++) {
+            float lv = lam[y * d->in_w + x];
+            if (lv <= 0.0f) continue;
+            o_small_rng rng = o_pixel_rng(p->seed, (int32_t)x, (int32_t)y);
+            o_poisson P = o_poisson_new((double)lv);
+            uint32_t q = o_f64_to_u32(o_poisson_sample(&P, o_small_next_v, &rng));
+            for (uint32_t g = 0; g < q; g++) {
+                float cx = (float)x + o_uniform_sample(&uni, &rng);
+                float cy = (float)y + o_uniform_sample(&uni, &rng);
+                float radius = o_radius_sample(p, &rng);
+                if (radius > d->rm) radius = d->rm;
+                if (radius <= 0.0f) continue;
+                float ro = radius * zoom;
+                if (ro <= 0.0f) continue;
+                float rsq = ro * ro;
+                g_tot++;
+                for (uint32_t k = 0; k < n; k++) {
+                    float tx = (cx * zoom) + offsets[2 * k];
+                    float ty = (cy * zoom) + offsets[2 * k + 1];
+                    int32_t xa, xb, ya, yb;
+                    if (!o_bounds(tx, ro, (int32_t)out_w, &xa, &xb)) continue;
+                    px_tot++;
+                    if (!o_bounds(ty, ro, (int32_t)out_h, &ya, &yb)) continue;
+                    py_tot++;
+                    int64_t lane = k / 64;
+                    uint64_t bm = 1ull << (k % 64);
+                    for (int32_t oy = ya; oy <= yb; oy++) {
+                        float dy = ((float)oy + 0.5f) - ty;
+                        float dysq = dy * dy;
+                        if (dysq > rsq) continue;
+                        for (int32_t ox = xa; ox <= xb; ox++) {
+                            float dx = ((float)ox + 0.5f) - tx;
+                            if (dx * dx + dysq <= rsq) {
+                                h_tot++;
+                                __atomic_fetch_or(&bits[((int64_t)oy * out_w + ox) * lanes + lane], bm, __ATOMIC_RELAXED);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (stats) { stats[0] = g_tot; stats[1] = count ? px_tot : 0; stats[2] = count ? py_tot : 0; stats[3] = count ? h_tot : 0; }
+    return 0;
+}
