@@ -130,29 +130,45 @@ fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_der
     return FG_OK;
 }
 
-void sorted_offset_table(const float *h_offs, uint32_t n, float4 *table) {
-    std::vector<float4> t(n);
+size_t grain_table_bytes(uint32_t n) { return (size_t)n * sizeof(float4) + (kGwBucketCount + 1) * sizeof(int); }
+
+void grain_table(const float *h_offs, uint32_t n, void *blob) {
+    struct Entry {
+        float fx;
+        float4 e;
+    };
+    std::vector<Entry> t(n);
     for (uint32_t k = 0; k < n; k++) {
-        float ox = h_offs[2 * k], oy = h_offs[2 * k + 1];
-        float fx = ox - std::floor(ox);
+        const float ox = h_offs[2 * k], oy = h_offs[2 * k + 1];
+        float fx = ox - std::floor(ox), fy = oy - std::floor(oy);
         if (!(fx < 1.0f)) fx = 0.0f;  // a tiny negative offset can round up to 1; cyclically that is 0
+        if (!(fy < 1.0f)) fy = 0.0f;
         int kb = (int)k;
         float kf;
         std::memcpy(&kf, &kb, 4);
-        t[k] = make_float4(fx, ox, oy, kf);
+        t[k] = Entry{fx, make_float4(fy, ox, oy, kf)};
     }
-    std::stable_sort(t.begin(), t.end(), [](const float4 &a, const float4 &b) { return a.x < b.x; });
-    std::copy(t.begin(), t.end(), table);
+    std::stable_sort(t.begin(), t.end(), [](const Entry &a, const Entry &b) { return a.fx < b.fx; });
+    float4 *entries = reinterpret_cast<float4 *>(blob);
+    int *bstart = reinterpret_cast<int *>(entries + n);
+    for (uint32_t k = 0; k < n; k++) entries[k] = t[k].e;
+    uint32_t j = 0;
+    for (int b = 0; b <= kGwBucketCount; b++) {
+        const float v = (float)b / (float)kGwBucketCount;
+        while (j < n && t[j].fx < v) j++;
+        bstart[b] = b == kGwBucketCount ? (int)n : (int)j;
+    }
 }
 
 GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const float *h_offs, const float *d_lam,
-                             const float4 *d_table, float *d_out) {
+                             const void *d_table, float *d_out) {
     GrainwiseArgs a;
     std::memset(&a, 0, sizeof a);
     float ext[4];
     offset_extents(h_offs, p.n_samples, ext);
     a.lam = d_lam;
-    a.sorted_offs = d_table;
+    a.sorted_offs = reinterpret_cast<const float4 *>(d_table);
+    a.bucket_start = reinterpret_cast<const int *>(reinterpret_cast<const float4 *>(d_table) + p.n_samples);
     a.out = d_out;
     a.in_w = (int)d.input_width; a.in_h = (int)d.input_height;
     a.out_w = (int)d.output_width; a.out_h = (int)d.output_height;
@@ -248,11 +264,10 @@ static fg_status render_plane_sync(int algo, const float *lambda, const fg_param
         d_out = (float *)b_out.p;
     }
     if (algo == FG_ALGO_GRAIN) {
-        std::vector<float4> tab(p.n_samples);
-        sorted_offset_table(h_offs.data(), p.n_samples, tab.data());
-        FG_CUDA(b_offs.alloc(sizeof(float4) * p.n_samples, s), "alloc offsets");
-        FG_CUDA(cudaMemcpyAsync(b_offs.p, tab.data(), sizeof(float4) * p.n_samples, cudaMemcpyHostToDevice, s),
-                "offsets H2D");
+        std::vector<unsigned char> tab(grain_table_bytes(p.n_samples));
+        grain_table(h_offs.data(), p.n_samples, tab.data());
+        FG_CUDA(b_offs.alloc(tab.size(), s), "alloc offsets");
+        FG_CUDA(cudaMemcpyAsync(b_offs.p, tab.data(), tab.size(), cudaMemcpyHostToDevice, s), "offsets H2D");
         d_offs = (const float *)b_offs.p;
     } else if (!offs_dev) {
         FG_CUDA(b_offs.alloc(off_bytes, s), "alloc offsets");
@@ -266,7 +281,7 @@ static fg_status render_plane_sync(int algo, const float *lambda, const fg_param
         st = enqueue_pixelwise(d_lam, p, d, h_offs.data(), d_offs, d_out, (CellParam *)b_cells.p,
                                (unsigned long long *)b_diag.p, nullptr, s);
     } else {
-        GrainwiseArgs a = grainwise_args(p, d, h_offs.data(), d_lam, (const float4 *)d_offs, d_out);
+        GrainwiseArgs a = grainwise_args(p, d, h_offs.data(), d_lam, d_offs, d_out);
         st = enqueue_grainwise(a, s);
     }
     if (st != FG_OK) {
@@ -327,13 +342,12 @@ FG_API fg_status fg_render_grainwise_async(const float *d_lambda, const fg_param
     if (is_device_ptr(offsets)) return set_error(FG_ERR_INVALID, "offsets must be host memory");
     keep_pool_memory();
     cudaStream_t s = (cudaStream_t)stream;
-    std::vector<float4> tab(params->n_samples);
-    sorted_offset_table(offsets, params->n_samples, tab.data());
+    std::vector<unsigned char> tab(grain_table_bytes(params->n_samples));
+    grain_table(offsets, params->n_samples, tab.data());
     DevBuf b_offs;
-    FG_CUDA(b_offs.alloc(sizeof(float4) * params->n_samples, s), "alloc offsets");
-    FG_CUDA(cudaMemcpyAsync(b_offs.p, tab.data(), sizeof(float4) * params->n_samples, cudaMemcpyHostToDevice, s),
-            "offsets H2D");
-    GrainwiseArgs a = grainwise_args(*params, *derived, offsets, d_lambda, (const float4 *)b_offs.p, d_out);
+    FG_CUDA(b_offs.alloc(tab.size(), s), "alloc offsets");
+    FG_CUDA(cudaMemcpyAsync(b_offs.p, tab.data(), tab.size(), cudaMemcpyHostToDevice, s), "offsets H2D");
+    GrainwiseArgs a = grainwise_args(*params, *derived, offsets, d_lambda, b_offs.p, d_out);
     return enqueue_grainwise(a, s);
 }
 
@@ -374,17 +388,16 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
     FG_CUDA(b_lam.alloc(sizeof(float) * n_in * nplanes, s), "alloc lambda");
     FG_CUDA(b_out.alloc(sizeof(float) * n_out * nplanes, s), "alloc planes");
     FG_CUDA(b_rgb8.alloc(3 * n_out, s), "alloc rgb8");
-    std::vector<float4> tab;
+    std::vector<unsigned char> tab;
     if (algo == FG_ALGO_PIXEL) {
         FG_CUDA(b_offs.alloc(sizeof(float) * 2 * p.n_samples, s), "alloc offsets");
         FG_CUDA(cudaMemcpyAsync(b_offs.p, offs_in.data(), sizeof(float) * 2 * p.n_samples, cudaMemcpyHostToDevice, s),
                 "offsets H2D");
     } else {
-        tab.resize(p.n_samples);
-        sorted_offset_table(offs.data(), p.n_samples, tab.data());
-        FG_CUDA(b_offs.alloc(sizeof(float4) * p.n_samples, s), "alloc offsets");
-        FG_CUDA(cudaMemcpyAsync(b_offs.p, tab.data(), sizeof(float4) * p.n_samples, cudaMemcpyHostToDevice, s),
-                "offsets H2D");
+        tab.resize(grain_table_bytes(p.n_samples));
+        grain_table(offs.data(), p.n_samples, tab.data());
+        FG_CUDA(b_offs.alloc(tab.size(), s), "alloc offsets");
+        FG_CUDA(cudaMemcpyAsync(b_offs.p, tab.data(), tab.size(), cudaMemcpyHostToDevice, s), "offsets H2D");
     }
     float *d_lam = (float *)b_lam.p, *d_out = (float *)b_out.p;
     float *d_cb = nullptr, *d_cr = nullptr;
@@ -423,8 +436,7 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
             st = enqueue_pixelwise(d_lam + (size_t)c * n_in, p, d, offs_in.data(), (const float *)b_offs.p, d_plane,
                                    (CellParam *)b_cells.p, (unsigned long long *)b_diag.p, &e, s);
         } else {
-            GrainwiseArgs a = grainwise_args(p, d, offs.data(), d_lam + (size_t)c * n_in, (const float4 *)b_offs.p,
-                                             d_plane);
+            GrainwiseArgs a = grainwise_args(p, d, offs.data(), d_lam + (size_t)c * n_in, b_offs.p, d_plane);
             if (luma) {
                 a.out_rgb8 = (unsigned char *)b_rgb8.p;
                 a.cb = d_cb;

@@ -14,10 +14,11 @@
 //     draws their grains one per lane per step; valid grains are compacted into a 64-entry warp
 //     queue with a ballot, and every full batch of 32 is rasterised grain by grain by the whole warp;
 //   - the offsets are sorted by the fractional part of their x component.  An offset can put a
-//     pixel centre inside a grain's disk only if frac(czx + offx) lies within radius_out of 1/2, so
-//     only the cyclic interval of the sorted table around frac(1/2 - czx), widened by a rounding
-//     margin, is scanned -- the lanes stride over it, each entry still going through the exact
-//     reference test;
+//     pixel centre inside a grain's disk only if frac(czx + offx) lies within radius_out of 1/2
+//     (and likewise for y), so only the cyclic interval of the sorted table around frac(1/2 - czx),
+//     widened by a rounding margin, is examined: stage A flattens those (grain, offset) pairs over
+//     the lanes and filters them by the same test on the y fractions; stage B runs the reference's
+//     exact bounds() and centre tests on the compacted survivors, one pair per lane;
 //   - the lognormal radius is evaluated with the double-float exp (exp_f64_to_f32).
 // Bits are set with shared-memory atomicOr; OR is idempotent and commutative, so the result does not
 // depend on the order.
@@ -30,8 +31,8 @@ namespace fg {
 constexpr int kGwThreads = 512;
 constexpr int kGwWarps = kGwThreads / 32;
 constexpr int kGwQueue = 64;     // grains per warp queue (a full batch of 32 plus a partial step)
-constexpr int kGwPairs = 64;     // surviving (grain, offset) pairs per warp queue
-constexpr int kGwBuckets = 256;  // bucket index over the sorted offset fractions
+constexpr int kGwList = 256;     // surviving (grain, offset) pairs per warp list
+constexpr int kGwBuckets = kGwBucketCount;
 
 struct GwTile {
     int tx0, ty0, tile_w, words;
@@ -65,16 +66,19 @@ __device__ __forceinline__ bool gw_range(float c, float r, float lo_t, float hi_
     return a <= b;
 }
 
-// Stage B: the reference's centre tests and bit sets of one surviving (grain, offset) pair
-// (src/grainwise.rs:80-101), restricted to the tile.  P = (tx, ty, radius_out, k).
+// Stage B: the reference's exact bounds() on both axes, clipped to the tile, then its centre tests and
+// bit sets (src/grainwise.rs:69-101) for one (grain, offset) pair.  G = (czx, czy, radius_out, -),
+// e = (frac(offy), offx, offy, k).
 template <bool kSmall>
-__device__ __forceinline__ void gw_splat(const GwTile &T, unsigned int *mask, const float4 P) {
-    const float tx = P.x, ty = P.y, ro = P.z;
-    const int k = __float_as_int(P.w);
-    const float rsq = FG_FMUL(ro, ro);
+__device__ __forceinline__ void gw_splat(const GwTile &T, unsigned int *mask, const float4 G, const float4 e) {
+    const float ro = G.z;
+    const float ty = FG_FADD(G.y, e.z);
     float y0, y1, x0, x1;
     if (!gw_range<kSmall>(ty, ro, T.fty0, T.fty1m, y0, y1)) return;
+    const float tx = FG_FADD(G.x, e.y);
     if (!gw_range<kSmall>(tx, ro, T.ftx0, T.ftx1m, x0, x1)) return;
+    const float rsq = FG_FMUL(ro, ro);
+    const int k = __float_as_int(e.w);
     const unsigned bit = 1u << (k & 31);
     unsigned int *base = mask + (k >> 5);
     int row = (int)(y0 - T.fty0) * T.tile_w;
@@ -120,13 +124,29 @@ __device__ __forceinline__ uint2 gw_candidates(const int *bstart, int n, float c
     return make_uint2((unsigned)s0 | ((unsigned)e0 << 16), (unsigned)s1 | ((unsigned)e1 << 16));
 }
 
+// Stage B over the warp's survivor list: one (grain, offset) pair per lane.
+template <bool kSmall>
+__device__ __forceinline__ void gw_drain(const GwTile &T, unsigned int *mask, const float4 *tab, const float4 *q,
+                                         const unsigned *list, int &ln, int lane) {
+    for (int b = 0; b < ln; b += 32) {
+        if (b + lane < ln) {
+            const unsigned v = list[b + lane];
+            gw_splat<kSmall>(T, mask, q[v >> 16], tab[v & 0xFFFFu]);
+        }
+    }
+    ln = 0;
+    __syncwarp();
+}
+
 // Stage A over one batch of `count` queued grains: the (grain, candidate offset) pairs are flattened
-// across the lanes (every lane busy), each pair gets the exact bounds test clipped to the tile, and
-// the survivors are compacted into the warp's pair queue; full batches of 32 pairs run stage B.
+// across the lanes (every lane busy).  A pair can set a bit only if some pixel row lies within
+// radius_out of ty = czy + offy, i.e. only if frac(offy) lies within h = radius_out + margin of
+// cy = frac(1/2 - czy) on the unit circle; that test filters the pairs, and the survivors -- (grain,
+// table index) -- are compacted into the warp's list for the exact stage B.
 template <bool kSmall>
 __device__ __forceinline__ void gw_raster_batch(const GwTile &T, unsigned int *mask, const float4 *tab,
-                                                const float4 *q, const uint2 *qr, int count, int *cpre,
-                                                float4 *pq, int &pn, int lane) {
+                                                const float *fy, const float4 *q, const uint2 *qr, int count,
+                                                int *cpre, unsigned *list, int &ln, float eps, int lane) {
     int c = 0;
     if (lane < count) {
         const uint2 r = qr[lane];
@@ -145,49 +165,39 @@ __device__ __forceinline__ void gw_raster_batch(const GwTile &T, unsigned int *m
     for (int base = 0; base < total; base += 32) {
         const int t = base + lane;
         bool surv = false;
-        float4 P;
+        unsigned item = 0;
         if (t < total) {
             while (cpre[g + 1] <= t) g++;
             const uint2 r = qr[g];
             const int o = t - cpre[g];
             const int n0 = (int)(r.x >> 16) - (int)(r.x & 0xFFFFu);
             const int i = o < n0 ? (int)(r.x & 0xFFFFu) + o : (int)(r.y & 0xFFFFu) + (o - n0);
-            const float4 G = q[g];
-            const float4 e = tab[i];
-            const float ty = FG_FADD(G.y, e.z);
-            float a, b;
-            if (gw_range<kSmall>(ty, G.z, T.fty0, T.fty1m, a, b)) {
-                const float tx = FG_FADD(G.x, e.y);
-                if (gw_range<kSmall>(tx, G.z, T.ftx0, T.ftx1m, a, b)) {
-                    surv = true;
-                    P = make_float4(tx, ty, G.z, e.w);
-                }
-            }
+            const float2 gy = *reinterpret_cast<const float2 *>(&q[g].z);  // (radius_out, cy)
+            const float h = FG_FADD(gy.x, eps);
+            const float d = fabsf(FG_FSUB(fy[i], gy.y));
+            surv = d <= h || d >= FG_FSUB(1.0f, h);
+            item = ((unsigned)g << 16) | (unsigned)i;
         }
         const unsigned sb = __ballot_sync(0xffffffffu, surv);
-        if (surv) pq[pn + __popc(sb & ((1u << lane) - 1u))] = P;
-        pn += __popc(sb);
+        if (surv) list[ln + __popc(sb & ((1u << lane) - 1u))] = item;
+        ln += __popc(sb);
         __syncwarp();
-        if (pn >= 32) {
-            gw_splat<kSmall>(T, mask, pq[lane]);
-            __syncwarp();
-            if (lane + 32 < pn) pq[lane] = pq[lane + 32];
-            pn -= 32;
-            __syncwarp();
-        }
+        if (ln > kGwList - 32) gw_drain<kSmall>(T, mask, tab, q, list, ln, lane);
     }
+    gw_drain<kSmall>(T, mask, tab, q, list, ln, lane);
 }
 
 template <bool kSmall>
 __global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const GrainwiseArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float4 *tab = reinterpret_cast<float4 *>(smem_raw);                   // [n] sorted offsets
+    float4 *tab = reinterpret_cast<float4 *>(smem_raw);                   // [n] offsets, by frac(offx)
     float4 *queue = tab + a.n;                                            // [warps][kGwQueue] grains
-    float4 *pairs = queue + kGwWarps * kGwQueue;                          // [warps][kGwPairs] pairs
-    uint2 *qrange = reinterpret_cast<uint2 *>(pairs + kGwWarps * kGwPairs); // [warps][kGwQueue]
-    int *cpre = reinterpret_cast<int *>(qrange + kGwWarps * kGwQueue);    // [warps][33]
+    uint2 *qrange = reinterpret_cast<uint2 *>(queue + kGwWarps * kGwQueue); // [warps][kGwQueue]
+    unsigned *lists = reinterpret_cast<unsigned *>(qrange + kGwWarps * kGwQueue);  // [warps][kGwList]
+    float *fy = reinterpret_cast<float *>(lists + kGwWarps * kGwList);    // [n] frac(offy), table order
+    int *cpre = reinterpret_cast<int *>(fy + a.n);                        // [warps][33]
     int *bstart = cpre + kGwWarps * 33;                                   // [kGwBuckets + 1]
-    unsigned int *mask = reinterpret_cast<unsigned int *>(bstart + kGwBuckets + 3);  // 16-B aligned
+    unsigned int *mask = reinterpret_cast<unsigned int *>(bstart + kGwBuckets + 3);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     const int tx0 = blockIdx.x * a.tile_w, ty0 = blockIdx.y * a.tile_h;
@@ -203,18 +213,13 @@ __global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const Grainwis
     T.fty1m = (float)(ty1 - 1);
     const int tile_words = a.tile_w * a.tile_h * a.words;
 
-    for (int k = tid; k < a.n; k += kGwThreads) tab[k] = a.sorted_offs[k];
-    for (int t = tid; t < tile_words; t += kGwThreads) mask[t] = 0u;
-    if (tid <= kGwBuckets) {  // bucket index over the sorted fractions (read from global: tab is in flight)
-        const float v = (float)tid / (float)kGwBuckets;
-        int lo = 0, hi = a.n;
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (a.sorted_offs[mid].x < v) lo = mid + 1;
-            else hi = mid;
-        }
-        bstart[tid] = tid == kGwBuckets ? a.n : lo;
+    for (int k = tid; k < a.n; k += kGwThreads) {
+        const float4 e = a.sorted_offs[k];
+        tab[k] = e;
+        fy[k] = e.x;
     }
+    for (int t = tid; t < tile_words; t += kGwThreads) mask[t] = 0u;
+    for (int b = tid; b <= kGwBuckets; b += kGwThreads) bstart[b] = a.bucket_start[b];
     __syncthreads();
 
     // Input pixels whose grains can reach the tile.  A grain of input pixel x has its zoomed centre
@@ -222,20 +227,20 @@ __global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const Grainwis
     // |ox + 0.5 - (czx + offx)| <= radius_out + (rounding), with radius_out <= rm*zoom.  `reach`
     // adds 1/16 px to cover the f32 roundings (a few ulps of the coordinates).
     const float reach = FG_FMUL(a.rm, a.zoom) + 0.0625f;
-    const int ix0 = max(0, (int)floorf(((float)tx0 + 0.5f - reach - a.offx_max) / a.zoom) - 1);
+    const int ix0 = max(0, (int)ceilf(((float)tx0 + 0.5f - reach - a.offx_max) / a.zoom - 1.0f));
     const int ix1 = min(a.in_w, (int)floorf(((float)tx1 - 0.5f + reach - a.offx_min) / a.zoom) + 1);
-    const int iy0 = max(0, (int)floorf(((float)ty0 + 0.5f - reach - a.offy_max) / a.zoom) - 1);
+    const int iy0 = max(0, (int)ceilf(((float)ty0 + 0.5f - reach - a.offy_max) / a.zoom - 1.0f));
     const int iy1 = min(a.in_h, (int)floorf(((float)ty1 - 0.5f + reach - a.offy_min) / a.zoom) + 1);
     const int fw = max(0, ix1 - ix0), total = fw * max(0, iy1 - iy0);
     const UniformF32 U = uniform_f32_new(0.0f, 1.0f);
     const float zoom = a.zoom;
     float4 *q = queue + warp * kGwQueue;
     uint2 *qr = qrange + warp * kGwQueue;
-    float4 *pq = pairs + warp * kGwPairs;
+    unsigned *list = lists + warp * kGwList;
     int *wc = cpre + warp * 33;
 
     int qn = 0;  // warp-uniform grain-queue fill
-    int pn = 0;  // warp-uniform pair-queue fill
+    int ln = 0;  // warp-uniform survivor-list fill
     for (int base = warp * 32; base < total; base += kGwThreads) {
         // one footprint pixel per lane, Poisson set-up in step across the warp
         const int pi = base + lane;
@@ -266,7 +271,10 @@ __global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const Grainwis
                     const float ro = FG_FMUL(r, zoom);
                     if (ro > 0.0f) {
                         valid = true;
-                        G = make_float4(FG_FMUL(cx, zoom), FG_FMUL(cy, zoom), ro, 0.0f);
+                        const float czy = FG_FMUL(cy, zoom);
+                        float cyf = FG_FSUB(0.5f, FG_FSUB(czy, floorf(czy)));  // frac(1/2 - czy)
+                        if (cyf < 0.0f) cyf = FG_FADD(cyf, 1.0f);
+                        G = make_float4(FG_FMUL(cx, zoom), czy, ro, cyf);
                         R = gw_candidates(bstart, a.n, G.x, ro, a.frac_eps);
                     }
                 }
@@ -280,7 +288,7 @@ __global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const Grainwis
             qn += __popc(vb);
             __syncwarp();
             if (qn >= 32) {
-                gw_raster_batch<kSmall>(T, mask, tab, q, qr, 32, wc, pq, pn, lane);
+                gw_raster_batch<kSmall>(T, mask, tab, fy, q, qr, 32, wc, list, ln, a.frac_eps, lane);
                 __syncwarp();
                 if (lane + 32 < qn) {
                     q[lane] = q[lane + 32];
@@ -291,9 +299,7 @@ __global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const Grainwis
             }
         }
     }
-    if (qn > 0) gw_raster_batch<kSmall>(T, mask, tab, q, qr, qn, wc, pq, pn, lane);
-    __syncwarp();
-    if (lane < pn) gw_splat<kSmall>(T, mask, pq[lane]);
+    if (qn > 0) gw_raster_batch<kSmall>(T, mask, tab, fy, q, qr, qn, wc, list, ln, a.frac_eps, lane);
     __syncthreads();
 
     // popcount * (1/N) (src/grainwise.rs:114-122), optionally fused with the luma recombination.
@@ -326,8 +332,8 @@ __global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const Grainwis
 
 size_t grainwise_smem_bytes(const GrainwiseArgs &a) {
     return (size_t)a.n * sizeof(float4) + (size_t)kGwWarps * kGwQueue * sizeof(float4) +
-           (size_t)kGwWarps * kGwPairs * sizeof(float4) + (size_t)kGwWarps * kGwQueue * sizeof(uint2) +
-           ((size_t)kGwWarps * 33 + kGwBuckets + 3) * sizeof(int) +
+           (size_t)kGwWarps * kGwQueue * sizeof(uint2) + (size_t)kGwWarps * kGwList * sizeof(unsigned) +
+           (size_t)a.n * sizeof(float) + ((size_t)kGwWarps * 33 + kGwBuckets + 3) * sizeof(int) +
            (size_t)a.tile_w * a.tile_h * a.words * sizeof(unsigned int);
 }
 

@@ -20,10 +20,12 @@ PwPlan plan_pixelwise(const fg_params &p, const fg_derived &d, const float *h_of
 fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_derived &d, const float *h_offs_in,
                             const float *d_offs_in, float *d_out, CellParam *d_cells, unsigned long long *d_diag,
                             const EpilogueArgs *colour, cudaStream_t s);
-// The grain-wise offset table: entries (frac(offx), offx, offy, k) sorted by frac(offx).
-void sorted_offset_table(const float *h_offs, uint32_t n, float4 *table);
+// The grain-wise offset table: n entries (frac(offy), offx, offy, k) sorted by frac(offx), followed by
+// the bucket index over frac(offx) (kGwBucketCount + 1 ints).
+size_t grain_table_bytes(uint32_t n);
+void grain_table(const float *h_offs, uint32_t n, void *blob);
 GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const float *h_offs, const float *d_lam,
-                             const float4 *d_table, float *d_out);
+                             const void *d_table, float *d_out);
 fg_status enqueue_grainwise(const GrainwiseArgs &a, cudaStream_t s);
 
 }  // namespace fg

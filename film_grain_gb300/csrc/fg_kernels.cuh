@@ -43,9 +43,12 @@ struct PixelwiseArgs {
     double log_mu, log_sigma;
 };
 
+constexpr int kGwBucketCount = 256;  // bucket index over the frac(offx)-sorted offsets
+
 struct GrainwiseArgs {
     const float *lam;           // in_w x in_h
-    const float4 *sorted_offs;  // [n] (frac(offx), offx, offy, k as int bits), ascending frac(offx)
+    const float4 *sorted_offs;  // [n] (frac(offy), offx, offy, k as int bits), ascending frac(offx)
+    const int *bucket_start;    // [kGwBucketCount + 1]: first entry with frac(offx) >= b / kGwBucketCount
     float *out;                 // out_w x out_h f32 plane (may be null when out_rgb8 is used)
     unsigned char *out_rgb8;    // fused colour output (luma mode) or null
     const float *cb, *cr;       // luma mode: chroma planes at input size

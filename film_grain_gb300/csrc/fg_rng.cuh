@@ -138,6 +138,19 @@ FG_HD double u53_unit(uint64_t v) {
     uint64_t ex = (uint64_t)(1023 - 53 + e);
     return bits_f64((ex << 52) | mant);
 }
+// v * 2^-51 for |v| <= 2^51, built from integer operations only (exact).
+FG_HD double i51_scaled(int64_t v) {
+    if (v == 0) return 0.0;
+    const uint64_t sign = v < 0 ? 0x8000000000000000ull : 0ull;
+    const uint64_t a = v < 0 ? (uint64_t)(-v) : (uint64_t)v;
+#ifdef __CUDA_ARCH__
+    const int e = 63 - __clzll((long long)a);
+#else
+    const int e = 63 - __builtin_clzll(a);
+#endif
+    const uint64_t mant = (a << (52 - e)) & 0x000FFFFFFFFFFFFFull;  // e <= 51
+    return bits_f64(sign | ((uint64_t)(1023 - 51 + e) << 52) | mant);
+}
 // Standard f64 from one raw draw.
 FG_HD double std_f64_from(uint64_t raw) { return u53_unit(raw >> 11); }
 // Open01 f64 from one raw draw: [1,2) minus (1 - eps/2).
@@ -272,9 +285,12 @@ FG_HD double std_normal(Rng &rng) {
     for (;;) {
         uint64_t bits = rng.next();
         unsigned i = (unsigned)(bits & 0xffu);
-        double u = FG_DSUB(bits_f64((bits >> 12) | 0x4000000000000000ull), 3.0);
+        // u = (2 + m*2^-51) - 3 for the 52-bit m = bits >> 12, i.e. exactly (m - 2^51) * 2^-51,
+        // built from integer operations (the subtraction is exact in f64).
+        double u = i51_scaled((int64_t)(bits >> 12) - (int64_t)(1ull << 51));
         double x = FG_DMUL(u, zig_x(i));
-        if (fabs(x) < zig_x(i + 1)) return x;
+        // |x| < x_tab[i+1]: both non-negative doubles, so their bit patterns order like the values.
+        if ((f64_bits(x) & 0x7FFFFFFFFFFFFFFFull) < f64_bits(zig_x(i + 1))) return x;
         if (i == 0) {
             double xx = 1.0, yy = 0.0;
             while (FG_DMUL(-2.0, yy) < FG_DMUL(xx, xx)) {
