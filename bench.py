@@ -256,7 +256,7 @@ def main():
     sp = stream.cuda_stream
     offs = np.ascontiguousarray(derived.offsets if wl["algo"] == "grain" else derived.offsets_input, np.float32)
     fn = L.fg_render_grainwise_async if wl["algo"] == "grain" else L.fg_render_pixelwise_async
-    launches_per_plane = 1 if wl["algo"] == "grain" else 3  # pixel: cell table, tile kernel, epilogue
+    launches_per_plane = 2 if wl["algo"] == "grain" else 3  # grain: raster, popcount; pixel: cells, tiles, epilogue
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     ev = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in planes] for _ in range(args.steps)]

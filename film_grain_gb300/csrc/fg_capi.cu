@@ -161,7 +161,7 @@ void grain_table(const float *h_offs, uint32_t n, void *blob) {
 }
 
 GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const float *h_offs, const float *d_lam,
-                             const void *d_table, float *d_out) {
+                             const void *d_table, unsigned int *d_gmask) {
     GrainwiseArgs a;
     std::memset(&a, 0, sizeof a);
     float ext[4];
@@ -169,20 +169,23 @@ GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const floa
     a.lam = d_lam;
     a.sorted_offs = reinterpret_cast<const float4 *>(d_table);
     a.bucket_start = reinterpret_cast<const int *>(reinterpret_cast<const float4 *>(d_table) + p.n_samples);
-    a.out = d_out;
+    a.gmask = d_gmask;
     a.in_w = (int)d.input_width; a.in_h = (int)d.input_height;
     a.out_w = (int)d.output_width; a.out_h = (int)d.output_height;
     a.n = (int)p.n_samples;
     a.words = (a.n + 31) / 32;
-    int pix = std::max(1, 16384 / a.words);
-    int tw = 64;
-    while (tw > 1 && tw * tw > pix) tw >>= 1;
-    a.tile_w = tw;
-    a.tile_h = std::max(1, std::min(64, pix / tw));
+    // Input tile: its zoomed rectangle should fill about 64 KiB of mask words.
+    // floor(x0*zoom + tin*zoom) - floor(x0*zoom) <= ceil(tin*zoom), so that bounds the rectangle.
+    const int side = std::max(1, (int)std::floor(std::sqrt(16384.0 / a.words)));
+    const int tin = std::max(1, (int)std::floor(side / p.zoom));
+    a.tin_w = std::min(tin, a.in_w);
+    a.tin_h = std::min(tin, a.in_h);
+    a.rmax_w = std::max(1, std::min(a.out_w, (int)std::ceil(a.tin_w * (double)p.zoom)));
+    a.rmax_h = std::max(1, std::min(a.out_h, (int)std::ceil(a.tin_h * (double)p.zoom)));
     a.rm = d.rm;
     a.zoom = p.zoom;
     a.offx_min = ext[0]; a.offx_max = ext[1]; a.offy_min = ext[2]; a.offy_max = ext[3];
-    // Rounding margin of the candidate interval: each of the three f32 roundings between
+    // Rounding margin of the candidate intervals: each of the three f32 roundings between
     // czx + offx and the bounds() comparison moves a value by at most half an ulp of the largest
     // coordinate M; the fraction arithmetic adds a few 2^-24.
     const double M = (double)std::max(d.output_width, d.output_height) + 8.0 +
@@ -197,10 +200,32 @@ GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const floa
     return a;
 }
 
+size_t grainwise_mask_bytes(const fg_params &p, const fg_derived &d) {
+    return (size_t)d.output_width * d.output_height * ((p.n_samples + 31) / 32) * sizeof(unsigned int);
+}
+
 fg_status enqueue_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
     if (grainwise_smem_bytes(a) > 200 * 1024)
         return set_error(FG_ERR_UNSUPPORTED, "n_samples too large for the grain-wise tile");
+    FG_CUDA(cudaMemsetAsync(a.gmask, 0, (size_t)a.out_w * a.out_h * a.words * sizeof(unsigned int), s), "memset mask");
     FG_CUDA(launch_grainwise(a, s), "grainwise kernel");
+    return FG_OK;
+}
+
+fg_status enqueue_grainwise_epilogue(const GrainwiseArgs &a, float *d_out, int mode, unsigned char *d_rgb8,
+                                     const float *d_cb, const float *d_cr, cudaStream_t s) {
+    GrainwiseEpilogueArgs e;
+    std::memset(&e, 0, sizeof e);
+    e.gmask = a.gmask;
+    e.out = d_out;
+    e.out_rgb8 = d_rgb8;
+    e.cb = d_cb;
+    e.cr = d_cr;
+    e.out_w = a.out_w; e.out_h = a.out_h; e.in_w = a.in_w; e.in_h = a.in_h;
+    e.n = a.n;
+    e.words = a.words;
+    e.mode = mode;
+    FG_CUDA(launch_grainwise_epilogue(e, s), "grainwise epilogue");
     return FG_OK;
 }
 
@@ -281,8 +306,10 @@ static fg_status render_plane_sync(int algo, const float *lambda, const fg_param
         st = enqueue_pixelwise(d_lam, p, d, h_offs.data(), d_offs, d_out, (CellParam *)b_cells.p,
                                (unsigned long long *)b_diag.p, nullptr, s);
     } else {
-        GrainwiseArgs a = grainwise_args(p, d, h_offs.data(), d_lam, d_offs, d_out);
+        FG_CUDA(b_cells.alloc(grainwise_mask_bytes(p, d), s), "alloc sample masks");
+        GrainwiseArgs a = grainwise_args(p, d, h_offs.data(), d_lam, d_offs, (unsigned int *)b_cells.p);
         st = enqueue_grainwise(a, s);
+        if (st == FG_OK) st = enqueue_grainwise_epilogue(a, d_out, 0, nullptr, nullptr, nullptr, s);
     }
     if (st != FG_OK) {
         cudaStreamSynchronize(s);
@@ -344,11 +371,14 @@ FG_API fg_status fg_render_grainwise_async(const float *d_lambda, const fg_param
     cudaStream_t s = (cudaStream_t)stream;
     std::vector<unsigned char> tab(grain_table_bytes(params->n_samples));
     grain_table(offsets, params->n_samples, tab.data());
-    DevBuf b_offs;
+    DevBuf b_offs, b_mask;
     FG_CUDA(b_offs.alloc(tab.size(), s), "alloc offsets");
     FG_CUDA(cudaMemcpyAsync(b_offs.p, tab.data(), tab.size(), cudaMemcpyHostToDevice, s), "offsets H2D");
-    GrainwiseArgs a = grainwise_args(*params, *derived, offsets, d_lambda, b_offs.p, d_out);
-    return enqueue_grainwise(a, s);
+    FG_CUDA(b_mask.alloc(grainwise_mask_bytes(*params, *derived), s), "alloc sample masks");
+    GrainwiseArgs a = grainwise_args(*params, *derived, offsets, d_lambda, b_offs.p, (unsigned int *)b_mask.p);
+    st = enqueue_grainwise(a, s);
+    if (st == FG_OK) st = enqueue_grainwise_epilogue(a, d_out, 0, nullptr, nullptr, nullptr, s);
+    return st;
 }
 
 FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height, const fg_params *params,
@@ -408,10 +438,13 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
         FG_CUDA(cudaMemcpyAsync(d_cb, planes.data() + n_in, sizeof(float) * 2 * n_in, cudaMemcpyHostToDevice, s),
                 "chroma H2D");
     }
+    const size_t mask_bytes = algo == FG_ALGO_GRAIN ? grainwise_mask_bytes(p, d) : 0;
     if (algo == FG_ALGO_PIXEL) {
         FG_CUDA(b_cells.alloc(sizeof(CellParam) * n_in, s), "alloc cell table");
         FG_CUDA(b_diag.alloc(sizeof(unsigned long long) * 4, s), "alloc diag");
         FG_CUDA(cudaMemsetAsync(b_diag.p, 0, sizeof(unsigned long long) * 4, s), "memset diag");
+    } else {
+        FG_CUDA(b_cells.alloc(mask_bytes * nplanes, s), "alloc sample masks");
     }
     std::vector<float> norm(n_in), lam((size_t)n_in * nplanes);
     for (int c = 0; c < nplanes; c++) {
@@ -436,17 +469,12 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
             st = enqueue_pixelwise(d_lam + (size_t)c * n_in, p, d, offs_in.data(), (const float *)b_offs.p, d_plane,
                                    (CellParam *)b_cells.p, (unsigned long long *)b_diag.p, &e, s);
         } else {
-            GrainwiseArgs a = grainwise_args(p, d, offs.data(), d_lam + (size_t)c * n_in, b_offs.p, d_plane);
-            if (luma) {
-                a.out_rgb8 = (unsigned char *)b_rgb8.p;
-                a.cb = d_cb;
-                a.cr = d_cr;
-            }
+            unsigned int *plane_mask = (unsigned int *)((unsigned char *)b_cells.p + mask_bytes * c);
+            GrainwiseArgs a = grainwise_args(p, d, offs.data(), d_lam + (size_t)c * n_in, b_offs.p, plane_mask);
             st = enqueue_grainwise(a, s);
-            if (st == FG_OK && !luma && c == 2) {
-                cudaError_t e = launch_rgb_pack(d_out, d_out + n_out, d_out + 2 * n_out, (int)n_out,
-                                                (unsigned char *)b_rgb8.p, s);
-                if (e != cudaSuccess) st = cuda_error(e, "rgb pack");
+            if (st == FG_OK && c == nplanes - 1) {
+                a.gmask = (unsigned int *)b_cells.p;  // all planes' masks, consecutive
+                st = enqueue_grainwise_epilogue(a, nullptr, luma ? 1 : 2, (unsigned char *)b_rgb8.p, d_cb, d_cr, s);
             }
         }
         if (st != FG_OK) {

@@ -34,9 +34,12 @@ constexpr int kGwQueue = 64;     // grains per warp queue (a full batch of 32 pl
 constexpr int kGwList = 256;     // surviving (grain, offset) pairs per warp list
 constexpr int kGwBuckets = kGwBucketCount;
 
+// The CTA's shared-memory mask covers the output rectangle [rx0, rx0 + rw) x [ry0, ry0 + rh); bits of
+// other output pixels go straight to the global mask.
 struct GwTile {
-    int tx0, ty0, tile_w, words;
-    float ftx0, fty0, ftx1m, fty1m;  // tile bounds as floats: first and last column / row
+    int rx0, ry0, rw, rh, words, out_w;
+    float flast_x, flast_y;          // last output column / row as floats
+    unsigned int *gmask;             // out_w x out_h x words
 };
 
 // floor / ceil of an f32.  With kSmall (every coordinate within +-2^22) they are one directed-rounding
@@ -52,13 +55,11 @@ __device__ __forceinline__ float gw_ceil(float v) {
     return ceilf(v);
 }
 
-// bounds(center, radius, limit) (src/grainwise.rs:126-142) intersected with the tile's rows or
-// columns [lo_t, hi_t] (a subset of [0, limit-1]): with lo = ceil((c - r) - 0.5) and
-// hi = floor((c + r) - 0.5), the reference yields Some iff lo <= hi, lo <= limit-1 and hi >= 0, and
-// then clamps to [0, limit-1]; intersecting that with [lo_t, hi_t] leaves [max(lo, lo_t),
-// min(hi, hi_t)], which is empty exactly when one of the reference's conditions fails or the range
-// misses the tile.  Coordinates stay below 2^24, so comparing integral floats is the reference's i32
-// comparison.
+// bounds(center, radius, limit) (src/grainwise.rs:126-142) as [max(lo, lo_t), min(hi, hi_t)] with
+// lo = ceil((c - r) - 0.5), hi = floor((c + r) - 0.5) and [lo_t, hi_t] = [0, limit-1]: the reference
+// yields Some iff lo <= hi, lo <= limit-1 and hi >= 0, and then clamps to [0, limit-1], which is
+// exactly this interval when it is non-empty.  Coordinates stay below 2^24, so comparing integral
+// floats is the reference's i32 comparison.
 template <bool kSmall>
 __device__ __forceinline__ bool gw_range(float c, float r, float lo_t, float hi_t, float &a, float &b) {
     a = fmaxf(gw_ceil<kSmall>(FG_FSUB(FG_FSUB(c, r), 0.5f)), lo_t);
@@ -66,30 +67,36 @@ __device__ __forceinline__ bool gw_range(float c, float r, float lo_t, float hi_
     return a <= b;
 }
 
-// Stage B: the reference's exact bounds() on both axes, clipped to the tile, then its centre tests and
-// bit sets (src/grainwise.rs:69-101) for one (grain, offset) pair.  G = (czx, czy, radius_out, -),
+// Stage B: the reference's exact bounds() on both axes, then its centre tests and bit sets
+// (src/grainwise.rs:69-101) for one (grain, offset) pair.  G = (czx, czy, radius_out, -),
 // e = (frac(offy), offx, offy, k).
 template <bool kSmall>
 __device__ __forceinline__ void gw_splat(const GwTile &T, unsigned int *mask, const float4 G, const float4 e) {
     const float ro = G.z;
     const float ty = FG_FADD(G.y, e.z);
     float y0, y1, x0, x1;
-    if (!gw_range<kSmall>(ty, ro, T.fty0, T.fty1m, y0, y1)) return;
+    if (!gw_range<kSmall>(ty, ro, 0.0f, T.flast_y, y0, y1)) return;
     const float tx = FG_FADD(G.x, e.y);
-    if (!gw_range<kSmall>(tx, ro, T.ftx0, T.ftx1m, x0, x1)) return;
+    if (!gw_range<kSmall>(tx, ro, 0.0f, T.flast_x, x0, x1)) return;
     const float rsq = FG_FMUL(ro, ro);
     const int k = __float_as_int(e.w);
     const unsigned bit = 1u << (k & 31);
-    unsigned int *base = mask + (k >> 5);
-    int row = (int)(y0 - T.fty0) * T.tile_w;
-    for (float oy = y0; oy <= y1; oy = FG_FADD(oy, 1.0f), row += T.tile_w) {
-        const float dy = FG_FSUB(FG_FADD(oy, 0.5f), ty);
+    const int word = k >> 5;
+    int oy = (int)y0;
+    for (float fyv = y0; fyv <= y1; fyv = FG_FADD(fyv, 1.0f), oy++) {
+        const float dy = FG_FSUB(FG_FADD(fyv, 0.5f), ty);
         const float dysq = FG_FMUL(dy, dy);
         if (dysq > rsq) continue;
-        int col = (int)(x0 - T.ftx0);
-        for (float ox = x0; ox <= x1; ox = FG_FADD(ox, 1.0f), col++) {
-            const float dx = FG_FSUB(FG_FADD(ox, 0.5f), tx);
-            if (FG_FADD(FG_FMUL(dx, dx), dysq) <= rsq) atomicOr(base + (row + col) * T.words, bit);
+        int ox = (int)x0;
+        for (float fxv = x0; fxv <= x1; fxv = FG_FADD(fxv, 1.0f), ox++) {
+            const float dx = FG_FSUB(FG_FADD(fxv, 0.5f), tx);
+            if (FG_FADD(FG_FMUL(dx, dx), dysq) <= rsq) {
+                const int lx = ox - T.rx0, ly = oy - T.ry0;
+                if ((unsigned)lx < (unsigned)T.rw && (unsigned)ly < (unsigned)T.rh)
+                    atomicOr(mask + (ly * T.rw + lx) * T.words + word, bit);
+                else
+                    atomicOr(T.gmask + ((long long)oy * T.out_w + ox) * T.words + word, bit);
+            }
         }
     }
 }
@@ -200,38 +207,33 @@ __global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const Grainwis
     unsigned int *mask = reinterpret_cast<unsigned int *>(bstart + kGwBuckets + 3);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-    const int tx0 = blockIdx.x * a.tile_w, ty0 = blockIdx.y * a.tile_h;
-    const int tx1 = min(tx0 + a.tile_w, a.out_w), ty1 = min(ty0 + a.tile_h, a.out_h);
+    // This CTA's input tile and the output rectangle its mask covers (the zoomed tile).
+    const int ix0 = blockIdx.x * a.tin_w, iy0 = blockIdx.y * a.tin_h;
+    const int ix1 = min(ix0 + a.tin_w, a.in_w), iy1 = min(iy0 + a.tin_h, a.in_h);
     GwTile T;
-    T.tx0 = tx0;
-    T.ty0 = ty0;
-    T.tile_w = a.tile_w;
+    T.rx0 = min(a.out_w, (int)floorf((float)ix0 * a.zoom));
+    T.ry0 = min(a.out_h, (int)floorf((float)iy0 * a.zoom));
+    T.rw = min(a.rmax_w, min(a.out_w, (int)floorf((float)ix1 * a.zoom)) - T.rx0);
+    T.rh = min(a.rmax_h, min(a.out_h, (int)floorf((float)iy1 * a.zoom)) - T.ry0);
+    T.rw = max(T.rw, 0);
+    T.rh = max(T.rh, 0);
     T.words = a.words;
-    T.ftx0 = (float)tx0;
-    T.fty0 = (float)ty0;
-    T.ftx1m = (float)(tx1 - 1);
-    T.fty1m = (float)(ty1 - 1);
-    const int tile_words = a.tile_w * a.tile_h * a.words;
+    T.out_w = a.out_w;
+    T.flast_x = (float)(a.out_w - 1);
+    T.flast_y = (float)(a.out_h - 1);
+    T.gmask = a.gmask;
+    const int region_words = T.rw * T.rh * a.words;
 
     for (int k = tid; k < a.n; k += kGwThreads) {
         const float4 e = a.sorted_offs[k];
         tab[k] = e;
         fy[k] = e.x;
     }
-    for (int t = tid; t < tile_words; t += kGwThreads) mask[t] = 0u;
+    for (int t = tid; t < region_words; t += kGwThreads) mask[t] = 0u;
     for (int b = tid; b <= kGwBuckets; b += kGwThreads) bstart[b] = a.bucket_start[b];
     __syncthreads();
 
-    // Input pixels whose grains can reach the tile.  A grain of input pixel x has its zoomed centre
-    // czx in [x*zoom, (x+1)*zoom]; it can set a bit of tile column ox only if
-    // |ox + 0.5 - (czx + offx)| <= radius_out + (rounding), with radius_out <= rm*zoom.  `reach`
-    // adds 1/16 px to cover the f32 roundings (a few ulps of the coordinates).
-    const float reach = FG_FMUL(a.rm, a.zoom) + 0.0625f;
-    const int ix0 = max(0, (int)ceilf(((float)tx0 + 0.5f - reach - a.offx_max) / a.zoom - 1.0f));
-    const int ix1 = min(a.in_w, (int)floorf(((float)tx1 - 0.5f + reach - a.offx_min) / a.zoom) + 1);
-    const int iy0 = max(0, (int)ceilf(((float)ty0 + 0.5f - reach - a.offy_max) / a.zoom - 1.0f));
-    const int iy1 = min(a.in_h, (int)floorf(((float)ty1 - 0.5f + reach - a.offy_min) / a.zoom) + 1);
-    const int fw = max(0, ix1 - ix0), total = fw * max(0, iy1 - iy0);
+    const int fw = ix1 - ix0, total = fw * (iy1 - iy0);
     const UniformF32 U = uniform_f32_new(0.0f, 1.0f);
     const float zoom = a.zoom;
     float4 *q = queue + warp * kGwQueue;
@@ -302,31 +304,53 @@ __global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const Grainwis
     if (qn > 0) gw_raster_batch<kSmall>(T, mask, tab, fy, q, qr, qn, wc, list, ln, a.frac_eps, lane);
     __syncthreads();
 
-    // popcount * (1/N) (src/grainwise.rs:114-122), optionally fused with the luma recombination.
-    const float inv_samples = FG_FDIV(1.0f, (float)(a.n > 0 ? a.n : 1));
-    const int tw = tx1 - tx0, th = ty1 - ty0;
-    for (int t = tid; t < tw * th; t += kGwThreads) {
-        const int lx = t % tw, ly = t / tw;
-        const unsigned int *m = mask + (ly * a.tile_w + lx) * a.words;
-        unsigned c = 0;
-        for (int w = 0; w < a.words; w++) c += __popc(m[w]);
-        const float v = FG_FMUL((float)c, inv_samples);
-        const int ox = tx0 + lx, oy = ty0 + ly;
-        const long long idx = (long long)oy * a.out_w + ox;
-        if (a.out) a.out[idx] = v;
-        if (a.out_rgb8) {
-            float cbv, crv;
-            if (a.in_w == a.out_w && a.in_h == a.out_h) {
-                cbv = a.cb[idx];
-                crv = a.cr[idx];
-            } else {
-                const float sxs = FG_FDIV((float)a.in_w, (float)a.out_w), sys = FG_FDIV((float)a.in_h, (float)a.out_h);
-                const long long src = (long long)nearest_src(oy, sys, a.in_h) * a.in_w + nearest_src(ox, sxs, a.in_w);
-                cbv = a.cb[src];
-                crv = a.cr[src];
-            }
-            luma_rgb8(v, cbv, crv, a.out_rgb8 + 3 * idx);
+    // OR the rectangle's words into the global mask (other CTAs' spills land there too).
+    for (int t = tid; t < region_words; t += kGwThreads) {
+        const unsigned v = mask[t];
+        if (v) {
+            const int w = t % a.words, px = t / a.words;
+            const int lx = px % T.rw, ly = px / T.rw;
+            atomicOr(a.gmask + ((long long)(T.ry0 + ly) * a.out_w + (T.rx0 + lx)) * a.words + w, v);
         }
+    }
+}
+
+// popcount * (1/N) of the sample masks (src/grainwise.rs:114-122), fused with the colour output:
+// mode 0 values only, 1 luma recombination + u8 (src/color.rs:75-96), 2 u8 pack of three planes
+// whose masks are consecutive (src/color.rs:101-113).
+__global__ void grainwise_epilogue_kernel(const GrainwiseEpilogueArgs a) {
+    const long long n = (long long)a.out_w * a.out_h;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float inv_samples = FG_FDIV(1.0f, (float)(a.n > 0 ? a.n : 1));
+    float v[3];
+    const int planes = a.mode == 2 ? 3 : 1;
+    for (int c = 0; c < planes; c++) {
+        const unsigned int *m = a.gmask + ((long long)c * n + i) * a.words;
+        unsigned cnt = 0;
+        for (int w = 0; w < a.words; w++) cnt += __popc(m[w]);
+        v[c] = FG_FMUL((float)cnt, inv_samples);
+        if (a.out) a.out[(long long)c * n + i] = v[c];
+    }
+    if (!a.out_rgb8) return;
+    unsigned char *o = a.out_rgb8 + 3 * i;
+    if (a.mode == 1) {
+        const int ox = (int)(i % a.out_w), oy = (int)(i / a.out_w);
+        float cbv, crv;
+        if (a.in_w == a.out_w && a.in_h == a.out_h) {
+            cbv = a.cb[i];
+            crv = a.cr[i];
+        } else {
+            const float sxs = FG_FDIV((float)a.in_w, (float)a.out_w), sys = FG_FDIV((float)a.in_h, (float)a.out_h);
+            const long long src = (long long)nearest_src(oy, sys, a.in_h) * a.in_w + nearest_src(ox, sxs, a.in_w);
+            cbv = a.cb[src];
+            crv = a.cr[src];
+        }
+        luma_rgb8(v[0], cbv, crv, o);
+    } else if (a.mode == 2) {
+        o[0] = to_u8(v[0]);
+        o[1] = to_u8(v[1]);
+        o[2] = to_u8(v[2]);
     }
 }
 
@@ -334,12 +358,12 @@ size_t grainwise_smem_bytes(const GrainwiseArgs &a) {
     return (size_t)a.n * sizeof(float4) + (size_t)kGwWarps * kGwQueue * sizeof(float4) +
            (size_t)kGwWarps * kGwQueue * sizeof(uint2) + (size_t)kGwWarps * kGwList * sizeof(unsigned) +
            (size_t)a.n * sizeof(float) + ((size_t)kGwWarps * 33 + kGwBuckets + 3) * sizeof(int) +
-           (size_t)a.tile_w * a.tile_h * a.words * sizeof(unsigned int);
+           (size_t)a.rmax_w * a.rmax_h * a.words * sizeof(unsigned int);
 }
 
 cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
     const size_t smem = grainwise_smem_bytes(a);
-    dim3 grid((a.out_w + a.tile_w - 1) / a.tile_w, (a.out_h + a.tile_h - 1) / a.tile_h);
+    dim3 grid((a.in_w + a.tin_w - 1) / a.tin_w, (a.in_h + a.tin_h - 1) / a.tin_h);
     if (grid.x == 0 || grid.y == 0) return cudaSuccess;
     // The directed-rounding floor/ceil needs every bounds() argument within +-2^22.
     const float span = (float)max(a.out_w, a.out_h) + fmaxf(fmaxf(-a.offx_min, a.offx_max), fmaxf(-a.offy_min, a.offy_max)) +
@@ -354,6 +378,13 @@ cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
         if (e != cudaSuccess) return e;
         grainwise_kernel<false><<<grid, kGwThreads, smem, s>>>(a);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grainwise_epilogue(const GrainwiseEpilogueArgs &a, cudaStream_t s) {
+    const long long n = (long long)a.out_w * a.out_h;
+    if (n <= 0) return cudaSuccess;
+    grainwise_epilogue_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

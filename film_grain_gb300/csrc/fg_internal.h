@@ -25,7 +25,10 @@ fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_der
 size_t grain_table_bytes(uint32_t n);
 void grain_table(const float *h_offs, uint32_t n, void *blob);
 GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const float *h_offs, const float *d_lam,
-                             const void *d_table, float *d_out);
+                             const void *d_table, unsigned int *d_gmask);
+size_t grainwise_mask_bytes(const fg_params &p, const fg_derived &d);
 fg_status enqueue_grainwise(const GrainwiseArgs &a, cudaStream_t s);
+fg_status enqueue_grainwise_epilogue(const GrainwiseArgs &a, float *d_out, int mode, unsigned char *d_rgb8,
+                                     const float *d_cb, const float *d_cr, cudaStream_t s);
 
 }  // namespace fg

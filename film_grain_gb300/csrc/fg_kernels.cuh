@@ -49,19 +49,29 @@ struct GrainwiseArgs {
     const float *lam;           // in_w x in_h
     const float4 *sorted_offs;  // [n] (frac(offy), offx, offy, k as int bits), ascending frac(offx)
     const int *bucket_start;    // [kGwBucketCount + 1]: first entry with frac(offx) >= b / kGwBucketCount
-    float *out;                 // out_w x out_h f32 plane (may be null when out_rgb8 is used)
-    unsigned char *out_rgb8;    // fused colour output (luma mode) or null
-    const float *cb, *cr;       // luma mode: chroma planes at input size
+    unsigned int *gmask;        // out_w x out_h x words sample masks (zeroed before the launch)
     int in_w, in_h, out_w, out_h;
     int n, words;               // words = ceil(n/32)
-    int tile_w, tile_h;
+    int tin_w, tin_h;           // input tile of one CTA
+    int rmax_w, rmax_h;         // bound of the zoomed tile rectangle held in shared memory
     float rm, zoom;
     float offx_min, offx_max, offy_min, offy_max;
-    float frac_eps;             // rounding margin of the candidate-offset interval
+    float frac_eps;             // rounding margin of the candidate-offset intervals
     unsigned long long seed;
     int lognorm;
     float radius_mean;
     double log_mu, log_sigma;
+};
+
+// popcount / colour epilogue of the grain-wise path.
+struct GrainwiseEpilogueArgs {
+    const unsigned int *gmask;  // planes x out_w x out_h x words
+    float *out;                 // planes x out_w x out_h values (may be null)
+    unsigned char *out_rgb8;    // null, or u8 RGB (mode 1 / 2)
+    const float *cb, *cr;       // luma: chroma planes at input size
+    int out_w, out_h, in_w, in_h;
+    int n, words;
+    int mode;                   // 0 values of one plane, 1 luma recombination, 2 pack of three planes
 };
 
 // Epilogue of the pixel-wise path: counts -> value (and optional colour packing).
@@ -80,6 +90,7 @@ cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, size_t smem, cudaS
 size_t pixelwise_smem_bytes();
 cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s);
 size_t grainwise_smem_bytes(const GrainwiseArgs &a);
+cudaError_t launch_grainwise_epilogue(const GrainwiseEpilogueArgs &a, cudaStream_t s);
 cudaError_t launch_epilogue(const EpilogueArgs &a, cudaStream_t s);
 cudaError_t launch_rgb_pack(const float *p0, const float *p1, const float *p2, int n, unsigned char *out,
                             cudaStream_t s);
