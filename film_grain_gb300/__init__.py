@@ -149,6 +149,7 @@ SIGNATURES = {
     "fg_render_grainwise": (ctypes.c_int, [_vp, _P(_ParamsC), _P(_DerivedC), _vp, _vp, _vp, _vp]),
     "fg_render_pixelwise_async": (ctypes.c_int, [_vp, _P(_ParamsC), _P(_DerivedC), _vp, _vp, _vp]),
     "fg_render_grainwise_async": (ctypes.c_int, [_vp, _P(_ParamsC), _P(_DerivedC), _vp, _vp, _vp]),
+    "fg_render_pixelwise_noalloc": (ctypes.c_int, [_vp, _P(_ParamsC), _P(_DerivedC), _vp, _vp, _vp]),
     "fg_render_image": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, _P(_ParamsC), _vp, _P(_StatsC), _vp,
                                        _vp]),
     "fg_dry_run": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, _P(_ParamsC), _P(_StatsC)]),

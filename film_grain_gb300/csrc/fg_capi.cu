@@ -51,7 +51,7 @@ void offset_extents(const float *offs, uint32_t n, float ext[4]) {
     }
 }
 
-static fg_status check_common(const fg_params *p, const fg_derived *d) {
+fg_status check_render_args(const fg_params *p, const fg_derived *d) {
     if (!p || !d) return set_error(FG_ERR_INVALID, "null params or derived");
     if (d->input_width <= 0 || d->input_height <= 0 || d->output_width <= 0 || d->output_height <= 0)
         return set_error(FG_ERR_INVALID, "plane dimensions must be positive");
@@ -258,7 +258,7 @@ static void keep_pool_memory() {
 // Shared body of the synchronous integrator entry points.
 static fg_status render_plane_sync(int algo, const float *lambda, const fg_params *params, const fg_derived *derived,
                                    const float *offsets, float *out, const volatile int32_t *cancel, void *stream) {
-    fg_status st = check_common(params, derived);
+    fg_status st = check_render_args(params, derived);
     if (st != FG_OK) return st;
     if (!lambda || !offsets || !out) return set_error(FG_ERR_INVALID, "null buffer");
     if (cancelled(cancel)) return set_error(FG_ERR_CANCELLED, "cancelled");
@@ -343,7 +343,7 @@ FG_API fg_status fg_render_grainwise(const float *lambda, const fg_params *param
 
 FG_API fg_status fg_render_pixelwise_async(const float *d_lambda, const fg_params *params, const fg_derived *derived,
                                            const float *offsets_input, float *d_out, void *stream) {
-    fg_status st = check_common(params, derived);
+    fg_status st = check_render_args(params, derived);
     if (st != FG_OK) return st;
     if (!d_lambda || !offsets_input || !d_out) return set_error(FG_ERR_INVALID, "null buffer");
     if (is_device_ptr(offsets_input)) return set_error(FG_ERR_INVALID, "offsets_input must be host memory");
@@ -363,7 +363,7 @@ FG_API fg_status fg_render_pixelwise_async(const float *d_lambda, const fg_param
 
 FG_API fg_status fg_render_grainwise_async(const float *d_lambda, const fg_params *params, const fg_derived *derived,
                                            const float *offsets, float *d_out, void *stream) {
-    fg_status st = check_common(params, derived);
+    fg_status st = check_render_args(params, derived);
     if (st != FG_OK) return st;
     if (!d_lambda || !offsets || !d_out) return set_error(FG_ERR_INVALID, "null buffer");
     if (is_device_ptr(offsets)) return set_error(FG_ERR_INVALID, "offsets must be host memory");
@@ -400,7 +400,7 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
     std::vector<float> offs(2 * (size_t)p.n_samples), offs_in(2 * (size_t)p.n_samples);
     fg_status st = derive(p, cw, ch, &d, offs.data(), offs_in.data());
     if (st != FG_OK) return st;
-    st = check_common(params, &d);
+    st = check_render_args(params, &d);
     if (st != FG_OK) return st;
     const int32_t algo = choose_algorithm(p, d);
     const bool luma = p.color_mode == FG_COLOR_LUMA;

@@ -14,6 +14,7 @@ struct PwPlan {
 };
 
 fg_status cuda_error(cudaError_t e, const char *what);
+fg_status check_render_args(const fg_params *p, const fg_derived *d);
 bool is_device_ptr(const void *p);
 void offset_extents(const float *offs, uint32_t n, float ext[4]);
 PwPlan plan_pixelwise(const fg_params &p, const fg_derived &d, const float *h_offs_in);

@@ -164,6 +164,22 @@ FG_API fg_status fg_render_grainwise_async(const float *d_lambda, const fg_param
                                            const fg_derived *derived, const float *d_offsets, float *d_out,
                                            void *stream);
 
+/* Pixel-wise render that allocates no device memory.  No counterpart in the crate: it exists for
+ * callers that may not allocate GPU memory themselves (a host that budgets all device memory and
+ * only lends a plug-in its own buffers, or a real-time preview loop that cannot afford cudaMalloc /
+ * cudaFree between frames).  d_lambda and d_out are device memory owned by the caller; offsets_input
+ * is host memory.  The kernel's scratch is one fixed-size array compiled into this library (present
+ * on every GPU that loads it, until process exit), so the call is limited to input planes of at
+ * most FG_NOALLOC_MAX_INPUT_PIXELS pixels and N <= FG_NOALLOC_MAX_SAMPLES (FG_ERR_UNSUPPORTED
+ * beyond).  The first call on each device looks up the array's device address; make that first call
+ * before any stream capture.  Every call on a device shares the array, so calls whose work overlaps
+ * on the GPU (concurrent streams, or host threads) race; serialise them.  Enqueues on `stream`. */
+#define FG_NOALLOC_MAX_INPUT_PIXELS (512u * 512u)
+#define FG_NOALLOC_MAX_SAMPLES 4096u
+FG_API fg_status fg_render_pixelwise_noalloc(const float *d_lambda, const fg_params *params,
+                                             const fg_derived *derived, const float *offsets_input, float *d_out,
+                                             void *stream);
+
 /* ---------------------------------------------------------------------------------------------
  * Whole-image orchestration (render_with_input_image, src/lib.rs:78-84 / 134-173).
  * ------------------------------------------------------------------------------------------- */
