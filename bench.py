@@ -200,7 +200,7 @@ def run_reference(args, wl, rank):
         if wl["algo"] == "grain":
             v, _, desc, _ = cpu_grain_baseline(oracle, planes, wl, threads, count=False)
         else:
-            v, _, desc, _ = cpu_pixel_baseline(oracle, planes, wl, threads, rows=None if wl["w"] <= 256 else 16)
+            v, _, desc, _ = cpu_pixel_baseline(oracle, planes, wl, threads, rows=None if wl["w"] <= 256 else 2)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
@@ -353,7 +353,7 @@ def main():
             cpu_v, cpu_t, desc, counts = cpu_grain_baseline(oracle, planes, wl, threads)
         else:
             cpu_v, cpu_t, desc, _ = cpu_pixel_baseline(oracle, planes, wl, threads,
-                                                        rows=None if wl["w"] <= 256 else 8)
+                                                        rows=None if wl["w"] <= 256 else 2)
         line["cpu_baseline"] = {"value": cpu_v, "unit": "samples/s", "cores": threads, "kind": "port",
                                 "sample": desc, "seconds": cpu_t}
     if counts and wl["algo"] == "grain":
