@@ -45,6 +45,12 @@ WORKLOADS = {
     "pixel_luma_256": dict(desc="plain pixel-wise luma 256x256 ramp+noise, const r 0.12, N 64, zoom 1, seed 42",
                            w=256, h=256, mode="luma", algo="pixel", radius=0.12, dist="const", sd=0.0, zoom=1.0, n=64,
                            seed=42, image_seed=42),
+    "grain_rgb_512": dict(desc="profiling case: grain-wise RGB 512x512x3 blobs, lognormal r 0.05/0.025, N 128, zoom 2",
+                          w=512, h=512, mode="rgb", algo="grain", radius=0.05, dist="lognorm", sd=0.025, zoom=2.0,
+                          n=128, seed=42, image_seed=0),
+    "pixel_rgb_1024": dict(desc="profiling case: pixel-wise RGB 1024x1024x3 blobs, lognormal r 0.025/0.01, N 256",
+                           w=1024, h=1024, mode="rgb", algo="pixel", radius=0.025, dist="lognorm", sd=0.01, zoom=1.0,
+                           n=256, seed=42, image_seed=1),
     "pixel_rgb_4096": dict(desc="plain pixel-wise RGB 4096x4096x3 blobs, lognormal r 0.025/0.01, N 256, zoom 1",
                            w=4096, h=4096, mode="rgb", algo="pixel", radius=0.025, dist="lognorm", sd=0.01, zoom=1.0,
                            n=256, seed=42, image_seed=1),
@@ -222,6 +228,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="grain_rgb_1024", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-once", action="store_true",
+                    help="render plane 0 once after one warm-up render and exit (a small case for ncu captures)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     wl = WORKLOADS[args.workload]
@@ -271,6 +279,15 @@ def main():
                 raise RuntimeError(L.fg_last_error_message().decode())
             if i is not None:
                 ev[i][c][1].record(stream)
+
+    if args.profile_once:
+        for _ in range(2):
+            rc = fn(lam_dev[0].data_ptr(), params.c, derived._c, offs.ctypes.data, outs[0].data_ptr(), sp)
+            if rc != 0:
+                raise RuntimeError(L.fg_last_error_message().decode())
+        torch.cuda.synchronize()
+        log(f"profile-once: {args.workload} plane 0 rendered twice")
+        return
 
     for _ in range(args.warmup):
         step()

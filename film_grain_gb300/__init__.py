@@ -31,6 +31,7 @@ __all__ = [
     "RenderError", "ParamsError", "CancelledError", "GpuError", "derive_common", "default_cell_delta",
     "normalize_plane", "lambda_plane", "choose_algorithm", "render_pixelwise", "render_grainwise",
     "render_with_input_image", "dry_run_with_input_image", "lib", "pixelwise_diagnostics", "make_offsets",
+    "Batch", "BatchTuning",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -134,6 +135,22 @@ class _StatsC(ctypes.Structure):
                 ("sigma_ratio", ctypes.c_float), ("rm_ratio", ctypes.c_float)]
 
 
+class _BatchImageC(ctypes.Structure):
+    _fields_ = [("algo", ctypes.c_int32), ("params", ctypes.POINTER(_ParamsC)), ("derived", ctypes.POINTER(_DerivedC)),
+                ("offsets", ctypes.c_void_p), ("d_lambda", ctypes.c_void_p), ("d_out", ctypes.c_void_p),
+                ("h_lambda", ctypes.c_void_p)]
+
+
+class BatchTuning(ctypes.Structure):
+    """fg_batch_tuning: grain-wise tile mask budget, pixel-wise block edge, persistent CTAs per SM."""
+    _fields_ = [("grain_mask_words", ctypes.c_int32), ("pixel_max_block_log2", ctypes.c_int32),
+                ("ctas_per_sm", ctypes.c_int32)]
+
+    def __repr__(self):
+        return (f"BatchTuning(grain_mask_words={self.grain_mask_words}, "
+                f"pixel_max_block_log2={self.pixel_max_block_log2}, ctas_per_sm={self.ctas_per_sm})")
+
+
 # Every symbol include/film_grain_gb300.h declares, with its ctypes signature.
 _P = ctypes.POINTER
 _f32p = _P(ctypes.c_float)
@@ -156,6 +173,12 @@ SIGNATURES = {
     "fg_last_error_message": (ctypes.c_char_p, []),
     "fg_version": (ctypes.c_char_p, []),
     "fg_pixelwise_diagnostics": (None, [_P(ctypes.c_ulonglong)]),
+    "fg_batch_create": (ctypes.c_int, [_P(_BatchImageC), ctypes.c_int32, _P(BatchTuning), _P(ctypes.c_void_p)]),
+    "fg_batch_run": (ctypes.c_int, [ctypes.c_void_p, _vp]),
+    "fg_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "fg_batch_get_tuning": (ctypes.c_int, [ctypes.c_void_p, _P(BatchTuning)]),
+    "fg_batch_autotune": (ctypes.c_int, [_P(_BatchImageC), ctypes.c_int32, _vp, _P(BatchTuning),
+                                         _P(ctypes.c_float)]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -409,3 +432,87 @@ def dry_run_with_input_image(rgb_shape, params: Params) -> RenderStats:
     st = _StatsC()
     _raise(lib().fg_dry_run(rgb_shape[1], rgb_shape[0], ctypes.byref(params.c), ctypes.byref(st)))
     return _stats(st)
+
+
+# ------------------------------------------------------------------ batches (no counterpart in the crate)
+class Batch:
+    """Many images (pixel-wise and grain-wise mixed, uneven sizes) rendered by one persistent launch
+    behind a CUDA graph.  Each entry of ``images`` is (lam_cuda_tensor, params, derived, algo[, lam_host]);
+    ``outputs`` receives one torch CUDA tensor per image, rewritten by every ``run()``."""
+
+    def __init__(self, images, tuning: Optional[BatchTuning] = None):
+        import torch
+        self._keep = []
+        arr = (_BatchImageC * len(images))()
+        self.outputs = []
+        for k, item in enumerate(images):
+            lam, params, derived, algo = item[:4]
+            host = item[4] if len(item) > 4 else None
+            if not _is_torch_cuda(lam) or lam.dtype != torch.float32 or not lam.is_contiguous():
+                raise RenderError("batch lambda planes must be contiguous float32 CUDA tensors", _FG_INVALID)
+            out = torch.empty((derived.output_height, derived.output_width), dtype=torch.float32, device=lam.device)
+            offs = np.ascontiguousarray(derived.offsets_input if Algo(algo) == Algo.Pixel else derived.offsets,
+                                        np.float32)
+            hl = None if host is None else np.ascontiguousarray(host, np.float32)
+            self._keep += [lam, out, offs, hl, params, derived]
+            arr[k].algo = int(algo)
+            arr[k].params = ctypes.pointer(params.c)
+            arr[k].derived = ctypes.pointer(derived._c)
+            arr[k].offsets = offs.ctypes.data
+            arr[k].d_lambda = lam.data_ptr()
+            arr[k].d_out = out.data_ptr()
+            arr[k].h_lambda = hl.ctypes.data if hl is not None else None
+            self.outputs.append(out)
+        self._arr = arr
+        self._h = ctypes.c_void_p()
+        _raise(lib().fg_batch_create(arr, len(images), ctypes.byref(tuning) if tuning is not None else None,
+                                     ctypes.byref(self._h)))
+
+    def run(self, stream=None):
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _raise(lib().fg_batch_run(self._h, st))
+
+    @property
+    def tuning(self) -> BatchTuning:
+        t = BatchTuning()
+        _raise(lib().fg_batch_get_tuning(self._h, ctypes.byref(t)))
+        return t
+
+    def close(self):
+        if self._h:
+            lib().fg_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def autotune(images) -> Tuple[BatchTuning, float]:
+        """Fastest tuning for these images (each candidate is built and timed on the GPU)."""
+        import torch
+        arr = (_BatchImageC * len(images))()
+        keep = []
+        for k, item in enumerate(images):
+            lam, params, derived, algo = item[:4]
+            host = item[4] if len(item) > 4 else None
+            out = torch.empty((derived.output_height, derived.output_width), dtype=torch.float32, device=lam.device)
+            offs = np.ascontiguousarray(derived.offsets_input if Algo(algo) == Algo.Pixel else derived.offsets,
+                                        np.float32)
+            hl = None if host is None else np.ascontiguousarray(host, np.float32)
+            keep += [out, offs, hl]
+            arr[k].algo = int(algo)
+            arr[k].params = ctypes.pointer(params.c)
+            arr[k].derived = ctypes.pointer(derived._c)
+            arr[k].offsets = offs.ctypes.data
+            arr[k].d_lambda = lam.data_ptr()
+            arr[k].d_out = out.data_ptr()
+            arr[k].h_lambda = hl.ctypes.data if hl is not None else None
+        best = BatchTuning()
+        ms = ctypes.c_float()
+        _raise(lib().fg_batch_autotune(arr, len(images), torch.cuda.current_stream().cuda_stream, ctypes.byref(best),
+                                       ctypes.byref(ms)))
+        return best, ms.value

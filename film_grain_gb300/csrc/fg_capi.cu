@@ -67,12 +67,12 @@ fg_status check_render_args(const fg_params *p, const fg_derived *d) {
 }
 
 // Pixel-wise launch plan: the largest power-of-two block edge whose staged window fits.
-PwPlan plan_pixelwise(const fg_params &p, const fg_derived &d, const float *h_offs_in) {
+PwPlan plan_pixelwise(const fg_params &p, const fg_derived &d, const float *h_offs_in, int max_block_log2) {
     PwPlan pl;
     offset_extents(h_offs_in, p.n_samples, pl.ext);
     const float rm = d.rm, delta = d.delta;
     int b;
-    for (b = 4; b > -8; b--) {
+    for (b = max_block_log2; b > -8; b--) {
         float B = std::ldexp(1.0f, b);
         double wc = std::floor((B + 2.0 * rm) / delta) + 4.0;
         if (wc <= kPwEdgeMax && wc * wc <= kPwCellMax) break;
@@ -89,14 +89,8 @@ PwPlan plan_pixelwise(const fg_params &p, const fg_derived &d, const float *h_of
     return pl;
 }
 
-fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_derived &d, const float *h_offs_in,
-                            const float *d_offs_in, float *d_out, CellParam *d_cells, unsigned long long *d_diag,
-                            const EpilogueArgs *colour, cudaStream_t s) {
-    const int in_w = (int)d.input_width, in_h = (int)d.input_height;
-    const int out_w = (int)d.output_width, out_h = (int)d.output_height;
-    PwPlan pl = plan_pixelwise(p, d, h_offs_in);
-    FG_CUDA(launch_cell_params(d_lam, in_w, in_h, d.delta, d_cells, s), "cell params");
-    FG_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * (size_t)out_w * out_h, s), "memset");
+PixelwiseArgs pixelwise_args(const fg_params &p, const fg_derived &d, const PwPlan &pl, const float *d_lam,
+                             const CellParam *d_cells, const float *d_offs_in, float *d_out, unsigned long long *d_diag) {
     PixelwiseArgs a;
     std::memset(&a, 0, sizeof a);
     a.lam = d_lam;
@@ -104,7 +98,8 @@ fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_der
     a.offs = reinterpret_cast<const float2 *>(d_offs_in);
     a.out = d_out;
     a.diag = d_diag;
-    a.in_w = in_w; a.in_h = in_h; a.out_w = out_w; a.out_h = out_h;
+    a.in_w = (int)d.input_width; a.in_h = (int)d.input_height;
+    a.out_w = (int)d.output_width; a.out_h = (int)d.output_height;
     a.n = (int)p.n_samples;
     a.rm = d.rm;
     a.delta = d.delta;
@@ -119,6 +114,18 @@ fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_der
     a.radius_mean = p.radius_mean;
     a.log_mu = (double)p.radius_log_mu;
     a.log_sigma = (double)p.radius_log_sigma;
+    return a;
+}
+
+fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_derived &d, const float *h_offs_in,
+                            const float *d_offs_in, float *d_out, CellParam *d_cells, unsigned long long *d_diag,
+                            const EpilogueArgs *colour, cudaStream_t s) {
+    const int in_w = (int)d.input_width, in_h = (int)d.input_height;
+    const int out_w = (int)d.output_width, out_h = (int)d.output_height;
+    const PwPlan pl = plan_pixelwise(p, d, h_offs_in, 4);
+    FG_CUDA(launch_cell_params(d_lam, in_w, in_h, d.delta, d_cells, s), "cell params");
+    FG_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * (size_t)out_w * out_h, s), "memset");
+    const PixelwiseArgs a = pixelwise_args(p, d, pl, d_lam, d_cells, d_offs_in, d_out, d_diag);
     FG_CUDA(launch_pixelwise(a, pl.nby, pixelwise_smem_bytes(), s), "pixelwise kernel");
     EpilogueArgs e;
     if (colour) e = *colour;
@@ -161,7 +168,7 @@ void grain_table(const float *h_offs, uint32_t n, void *blob) {
 }
 
 GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const float *h_offs, const float *d_lam,
-                             const void *d_table, unsigned int *d_gmask) {
+                             const void *d_table, unsigned int *d_gmask, int mask_words) {
     GrainwiseArgs a;
     std::memset(&a, 0, sizeof a);
     float ext[4];
@@ -174,9 +181,9 @@ GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const floa
     a.out_w = (int)d.output_width; a.out_h = (int)d.output_height;
     a.n = (int)p.n_samples;
     a.words = (a.n + 31) / 32;
-    // Input tile: its zoomed rectangle should fill about 64 KiB of mask words.
+    // Input tile: its zoomed rectangle should fill about `mask_words` words of shared memory.
     // floor(x0*zoom + tin*zoom) - floor(x0*zoom) <= ceil(tin*zoom), so that bounds the rectangle.
-    const int side = std::max(1, (int)std::floor(std::sqrt(16384.0 / a.words)));
+    const int side = std::max(1, (int)std::floor(std::sqrt((double)mask_words / a.words)));
     const int tin = std::max(1, (int)std::floor(side / p.zoom));
     a.tin_w = std::min(tin, a.in_w);
     a.tin_h = std::min(tin, a.in_h);
@@ -307,7 +314,7 @@ static fg_status render_plane_sync(int algo, const float *lambda, const fg_param
                                (unsigned long long *)b_diag.p, nullptr, s);
     } else {
         FG_CUDA(b_cells.alloc(grainwise_mask_bytes(p, d), s), "alloc sample masks");
-        GrainwiseArgs a = grainwise_args(p, d, h_offs.data(), d_lam, d_offs, (unsigned int *)b_cells.p);
+        GrainwiseArgs a = grainwise_args(p, d, h_offs.data(), d_lam, d_offs, (unsigned int *)b_cells.p, 16384);
         st = enqueue_grainwise(a, s);
         if (st == FG_OK) st = enqueue_grainwise_epilogue(a, d_out, 0, nullptr, nullptr, nullptr, s);
     }
@@ -375,7 +382,7 @@ FG_API fg_status fg_render_grainwise_async(const float *d_lambda, const fg_param
     FG_CUDA(b_offs.alloc(tab.size(), s), "alloc offsets");
     FG_CUDA(cudaMemcpyAsync(b_offs.p, tab.data(), tab.size(), cudaMemcpyHostToDevice, s), "offsets H2D");
     FG_CUDA(b_mask.alloc(grainwise_mask_bytes(*params, *derived), s), "alloc sample masks");
-    GrainwiseArgs a = grainwise_args(*params, *derived, offsets, d_lambda, b_offs.p, (unsigned int *)b_mask.p);
+    GrainwiseArgs a = grainwise_args(*params, *derived, offsets, d_lambda, b_offs.p, (unsigned int *)b_mask.p, 16384);
     st = enqueue_grainwise(a, s);
     if (st == FG_OK) st = enqueue_grainwise_epilogue(a, d_out, 0, nullptr, nullptr, nullptr, s);
     return st;
@@ -470,7 +477,7 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
                                    (CellParam *)b_cells.p, (unsigned long long *)b_diag.p, &e, s);
         } else {
             unsigned int *plane_mask = (unsigned int *)((unsigned char *)b_cells.p + mask_bytes * c);
-            GrainwiseArgs a = grainwise_args(p, d, offs.data(), d_lam + (size_t)c * n_in, b_offs.p, plane_mask);
+            GrainwiseArgs a = grainwise_args(p, d, offs.data(), d_lam + (size_t)c * n_in, b_offs.p, plane_mask, 16384);
             st = enqueue_grainwise(a, s);
             if (st == FG_OK && c == nplanes - 1) {
                 a.gmask = (unsigned int *)b_cells.p;  // all planes' masks, consecutive

@@ -25,294 +25,15 @@
 #include "fg_kernels.cuh"
 #include "fg_rng.cuh"
 #include "fg_color.cuh"
+#include "fg_grainwise.cuh"
+#include "fg_internal.h"
 
 namespace fg {
 
-constexpr int kGwThreads = 512;
-constexpr int kGwWarps = kGwThreads / 32;
-constexpr int kGwQueue = 64;     // grains per warp queue (a full batch of 32 plus a partial step)
-constexpr int kGwList = 256;     // surviving (grain, offset) pairs per warp list
-constexpr int kGwBuckets = kGwBucketCount;
-
-// The CTA's shared-memory mask covers the output rectangle [rx0, rx0 + rw) x [ry0, ry0 + rh); bits of
-// other output pixels go straight to the global mask.
-struct GwTile {
-    int rx0, ry0, rw, rh, words, out_w;
-    float flast_x, flast_y;          // last output column / row as floats
-    unsigned int *gmask;             // out_w x out_h x words
-};
-
-// floor / ceil of an f32.  With kSmall (every coordinate within +-2^22) they are one directed-rounding
-// add and one exact subtract of 1.5 * 2^23, which stay on the FP32 pipes.
 template <bool kSmall>
-__device__ __forceinline__ float gw_floor(float v) {
-    if (kSmall) return __fsub_rn(__fadd_rd(v, 12582912.0f), 12582912.0f);
-    return floorf(v);
-}
-template <bool kSmall>
-__device__ __forceinline__ float gw_ceil(float v) {
-    if (kSmall) return __fsub_rn(__fadd_ru(v, 12582912.0f), 12582912.0f);
-    return ceilf(v);
-}
-
-// bounds(center, radius, limit) (src/grainwise.rs:126-142) as [max(lo, lo_t), min(hi, hi_t)] with
-// lo = ceil((c - r) - 0.5), hi = floor((c + r) - 0.5) and [lo_t, hi_t] = [0, limit-1]: the reference
-// yields Some iff lo <= hi, lo <= limit-1 and hi >= 0, and then clamps to [0, limit-1], which is
-// exactly this interval when it is non-empty.  Coordinates stay below 2^24, so comparing integral
-// floats is the reference's i32 comparison.
-template <bool kSmall>
-__device__ __forceinline__ bool gw_range(float c, float r, float lo_t, float hi_t, float &a, float &b) {
-    a = fmaxf(gw_ceil<kSmall>(FG_FSUB(FG_FSUB(c, r), 0.5f)), lo_t);
-    b = fminf(gw_floor<kSmall>(FG_FSUB(FG_FADD(c, r), 0.5f)), hi_t);
-    return a <= b;
-}
-
-// Stage B: the reference's exact bounds() on both axes, then its centre tests and bit sets
-// (src/grainwise.rs:69-101) for one (grain, offset) pair.  G = (czx, czy, radius_out, -),
-// e = (frac(offy), offx, offy, k).
-template <bool kSmall>
-__device__ __forceinline__ void gw_splat(const GwTile &T, unsigned int *mask, const float4 G, const float4 e) {
-    const float ro = G.z;
-    const float ty = FG_FADD(G.y, e.z);
-    float y0, y1, x0, x1;
-    if (!gw_range<kSmall>(ty, ro, 0.0f, T.flast_y, y0, y1)) return;
-    const float tx = FG_FADD(G.x, e.y);
-    if (!gw_range<kSmall>(tx, ro, 0.0f, T.flast_x, x0, x1)) return;
-    const float rsq = FG_FMUL(ro, ro);
-    const int k = __float_as_int(e.w);
-    const unsigned bit = 1u << (k & 31);
-    const int word = k >> 5;
-    int oy = (int)y0;
-    for (float fyv = y0; fyv <= y1; fyv = FG_FADD(fyv, 1.0f), oy++) {
-        const float dy = FG_FSUB(FG_FADD(fyv, 0.5f), ty);
-        const float dysq = FG_FMUL(dy, dy);
-        if (dysq > rsq) continue;
-        int ox = (int)x0;
-        for (float fxv = x0; fxv <= x1; fxv = FG_FADD(fxv, 1.0f), ox++) {
-            const float dx = FG_FSUB(FG_FADD(fxv, 0.5f), tx);
-            if (FG_FADD(FG_FMUL(dx, dx), dysq) <= rsq) {
-                const int lx = ox - T.rx0, ly = oy - T.ry0;
-                if ((unsigned)lx < (unsigned)T.rw && (unsigned)ly < (unsigned)T.rh)
-                    atomicOr(mask + (ly * T.rw + lx) * T.words + word, bit);
-                else
-                    atomicOr(T.gmask + ((long long)oy * T.out_w + ox) * T.words + word, bit);
-            }
-        }
-    }
-}
-
-// Candidate ranges of one grain in the sorted offset table: the entries whose frac(offx) lies in the
-// cyclic interval [c - h, c + h], c = frac(1/2 - czx), h = radius_out + margin, rounded out to whole
-// buckets of the index `bstart` (bstart[b] = first entry with frac >= b / kGwBuckets).  Entries the
-// rounding adds are harmless: every entry still goes through the exact reference test.  Packed as
-// (first | end << 16) for the two pieces of the cyclic interval.
-__device__ __forceinline__ uint2 gw_candidates(const int *bstart, int n, float czx, float ro, float eps) {
-    const float h = FG_FADD(ro, eps);
-    if (h >= 0.5f) return make_uint2((unsigned)n << 16, 0u);
-    const float fz = FG_FSUB(czx, floorf(czx));     // exact
-    float c = FG_FSUB(0.5f, fz);
-    if (c < 0.0f) c = FG_FADD(c, 1.0f);
-    const float lo = FG_FSUB(c, h), hi = FG_FADD(c, h);
-    const float nb = (float)kGwBuckets;
-    int s0, e0, s1 = 0, e1 = 0;
-    if (lo < 0.0f) {  // [0, hi] and [lo + 1, 1)
-        s0 = 0;
-        e0 = bstart[min(kGwBuckets - 1, (int)(hi * nb)) + 1];
-        s1 = bstart[min(kGwBuckets - 1, max(0, (int)(FG_FADD(lo, 1.0f) * nb)))];
-        e1 = n;
-    } else if (hi >= 1.0f) {  // [lo, 1) and [0, hi - 1]
-        s0 = bstart[min(kGwBuckets - 1, (int)(lo * nb))];
-        e0 = n;
-        e1 = bstart[min(kGwBuckets - 1, max(0, (int)(FG_FSUB(hi, 1.0f) * nb))) + 1];
-    } else {
-        s0 = bstart[min(kGwBuckets - 1, (int)(lo * nb))];
-        e0 = bstart[min(kGwBuckets - 1, (int)(hi * nb)) + 1];
-    }
-    return make_uint2((unsigned)s0 | ((unsigned)e0 << 16), (unsigned)s1 | ((unsigned)e1 << 16));
-}
-
-// Stage B over the warp's survivor list: one (grain, offset) pair per lane.
-template <bool kSmall>
-__device__ __forceinline__ void gw_drain(const GwTile &T, unsigned int *mask, const float4 *tab, const float4 *q,
-                                         const unsigned *list, int &ln, int lane) {
-    for (int b = 0; b < ln; b += 32) {
-        if (b + lane < ln) {
-            const unsigned v = list[b + lane];
-            gw_splat<kSmall>(T, mask, q[v >> 16], tab[v & 0xFFFFu]);
-        }
-    }
-    ln = 0;
-    __syncwarp();
-}
-
-// Stage A over one batch of `count` queued grains: the (grain, candidate offset) pairs are flattened
-// across the lanes (every lane busy).  A pair can set a bit only if some pixel row lies within
-// radius_out of ty = czy + offy, i.e. only if frac(offy) lies within h = radius_out + margin of
-// cy = frac(1/2 - czy) on the unit circle; that test filters the pairs, and the survivors -- (grain,
-// table index) -- are compacted into the warp's list for the exact stage B.
-template <bool kSmall>
-__device__ __forceinline__ void gw_raster_batch(const GwTile &T, unsigned int *mask, const float4 *tab,
-                                                const float *fy, const float4 *q, const uint2 *qr, int count,
-                                                int *cpre, unsigned *list, int &ln, float eps, int lane) {
-    int c = 0;
-    if (lane < count) {
-        const uint2 r = qr[lane];
-        c = (int)(r.x >> 16) - (int)(r.x & 0xFFFFu) + (int)(r.y >> 16) - (int)(r.y & 0xFFFFu);
-    }
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, c, o);
-        if (lane >= o) c += y;
-    }
-    const int total = __shfl_sync(0xffffffffu, c, 31);
-    cpre[lane + 1] = c;
-    if (lane == 0) cpre[0] = 0;
-    __syncwarp();
-    int g = 0;
-    for (int base = 0; base < total; base += 32) {
-        const int t = base + lane;
-        bool surv = false;
-        unsigned item = 0;
-        if (t < total) {
-            while (cpre[g + 1] <= t) g++;
-            const uint2 r = qr[g];
-            const int o = t - cpre[g];
-            const int n0 = (int)(r.x >> 16) - (int)(r.x & 0xFFFFu);
-            const int i = o < n0 ? (int)(r.x & 0xFFFFu) + o : (int)(r.y & 0xFFFFu) + (o - n0);
-            const float2 gy = *reinterpret_cast<const float2 *>(&q[g].z);  // (radius_out, cy)
-            const float h = FG_FADD(gy.x, eps);
-            const float d = fabsf(FG_FSUB(fy[i], gy.y));
-            surv = d <= h || d >= FG_FSUB(1.0f, h);
-            item = ((unsigned)g << 16) | (unsigned)i;
-        }
-        const unsigned sb = __ballot_sync(0xffffffffu, surv);
-        if (surv) list[ln + __popc(sb & ((1u << lane) - 1u))] = item;
-        ln += __popc(sb);
-        __syncwarp();
-        if (ln > kGwList - 32) gw_drain<kSmall>(T, mask, tab, q, list, ln, lane);
-    }
-    gw_drain<kSmall>(T, mask, tab, q, list, ln, lane);
-}
-
-template <bool kSmall>
-__global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const GrainwiseArgs a) {
+__global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const __grid_constant__ GrainwiseArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float4 *tab = reinterpret_cast<float4 *>(smem_raw);                   // [n] offsets, by frac(offx)
-    float4 *queue = tab + a.n;                                            // [warps][kGwQueue] grains
-    uint2 *qrange = reinterpret_cast<uint2 *>(queue + kGwWarps * kGwQueue); // [warps][kGwQueue]
-    unsigned *lists = reinterpret_cast<unsigned *>(qrange + kGwWarps * kGwQueue);  // [warps][kGwList]
-    float *fy = reinterpret_cast<float *>(lists + kGwWarps * kGwList);    // [n] frac(offy), table order
-    int *cpre = reinterpret_cast<int *>(fy + a.n);                        // [warps][33]
-    int *bstart = cpre + kGwWarps * 33;                                   // [kGwBuckets + 1]
-    unsigned int *mask = reinterpret_cast<unsigned int *>(bstart + kGwBuckets + 3);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-
-    // This CTA's input tile and the output rectangle its mask covers (the zoomed tile).
-    const int ix0 = blockIdx.x * a.tin_w, iy0 = blockIdx.y * a.tin_h;
-    const int ix1 = min(ix0 + a.tin_w, a.in_w), iy1 = min(iy0 + a.tin_h, a.in_h);
-    GwTile T;
-    T.rx0 = min(a.out_w, (int)floorf((float)ix0 * a.zoom));
-    T.ry0 = min(a.out_h, (int)floorf((float)iy0 * a.zoom));
-    T.rw = min(a.rmax_w, min(a.out_w, (int)floorf((float)ix1 * a.zoom)) - T.rx0);
-    T.rh = min(a.rmax_h, min(a.out_h, (int)floorf((float)iy1 * a.zoom)) - T.ry0);
-    T.rw = max(T.rw, 0);
-    T.rh = max(T.rh, 0);
-    T.words = a.words;
-    T.out_w = a.out_w;
-    T.flast_x = (float)(a.out_w - 1);
-    T.flast_y = (float)(a.out_h - 1);
-    T.gmask = a.gmask;
-    const int region_words = T.rw * T.rh * a.words;
-
-    for (int k = tid; k < a.n; k += kGwThreads) {
-        const float4 e = a.sorted_offs[k];
-        tab[k] = e;
-        fy[k] = e.x;
-    }
-    for (int t = tid; t < region_words; t += kGwThreads) mask[t] = 0u;
-    for (int b = tid; b <= kGwBuckets; b += kGwThreads) bstart[b] = a.bucket_start[b];
-    __syncthreads();
-
-    const int fw = ix1 - ix0, total = fw * (iy1 - iy0);
-    const UniformF32 U = uniform_f32_new(0.0f, 1.0f);
-    const float zoom = a.zoom;
-    float4 *q = queue + warp * kGwQueue;
-    uint2 *qr = qrange + warp * kGwQueue;
-    unsigned *list = lists + warp * kGwList;
-    int *wc = cpre + warp * 33;
-
-    int qn = 0;  // warp-uniform grain-queue fill
-    int ln = 0;  // warp-uniform survivor-list fill
-    for (int base = warp * 32; base < total; base += kGwThreads) {
-        // one footprint pixel per lane, Poisson set-up in step across the warp
-        const int pi = base + lane;
-        uint32_t left = 0;
-        int px = 0, py = 0;
-        Xoshiro rng = {0, 0, 0, 0};
-        if (pi < total) {
-            px = ix0 + pi % fw;
-            py = iy0 + pi / fw;
-            const float lv = a.lam[(long long)py * a.in_w + px];
-            if (lv > 0.0f) {
-                rng = pixel_rng(a.seed, px, py);
-                const PoissonParams P = poisson_new((double)lv);
-                left = poisson_sample(P, rng);
-            }
-        }
-        while (__any_sync(0xffffffffu, left > 0)) {
-            bool valid = false;
-            float4 G;
-            uint2 R;
-            if (left > 0) {
-                left--;
-                const float cx = FG_FADD((float)px, uniform_f32_from(U, rng.next()));
-                const float cy = FG_FADD((float)py, uniform_f32_from(U, rng.next()));
-                float r = a.lognorm ? lognormal_radius_f32(a.log_mu, a.log_sigma, rng) : a.radius_mean;
-                if (r > a.rm) r = a.rm;
-                if (r > 0.0f) {
-                    const float ro = FG_FMUL(r, zoom);
-                    if (ro > 0.0f) {
-                        valid = true;
-                        const float czy = FG_FMUL(cy, zoom);
-                        float cyf = FG_FSUB(0.5f, FG_FSUB(czy, floorf(czy)));  // frac(1/2 - czy)
-                        if (cyf < 0.0f) cyf = FG_FADD(cyf, 1.0f);
-                        G = make_float4(FG_FMUL(cx, zoom), czy, ro, cyf);
-                        R = gw_candidates(bstart, a.n, G.x, ro, a.frac_eps);
-                    }
-                }
-            }
-            const unsigned vb = __ballot_sync(0xffffffffu, valid);
-            if (valid) {
-                const int slot = qn + __popc(vb & ((1u << lane) - 1u));
-                q[slot] = G;
-                qr[slot] = R;
-            }
-            qn += __popc(vb);
-            __syncwarp();
-            if (qn >= 32) {
-                gw_raster_batch<kSmall>(T, mask, tab, fy, q, qr, 32, wc, list, ln, a.frac_eps, lane);
-                __syncwarp();
-                if (lane + 32 < qn) {
-                    q[lane] = q[lane + 32];
-                    qr[lane] = qr[lane + 32];
-                }
-                qn -= 32;
-                __syncwarp();
-            }
-        }
-    }
-    if (qn > 0) gw_raster_batch<kSmall>(T, mask, tab, fy, q, qr, qn, wc, list, ln, a.frac_eps, lane);
-    __syncthreads();
-
-    // OR the rectangle's words into the global mask (other CTAs' spills land there too).
-    for (int t = tid; t < region_words; t += kGwThreads) {
-        const unsigned v = mask[t];
-        if (v) {
-            const int w = t % a.words, px = t / a.words;
-            const int lx = px % T.rw, ly = px / T.rw;
-            atomicOr(a.gmask + ((long long)(T.ry0 + ly) * a.out_w + (T.rx0 + lx)) * a.words + w, v);
-        }
-    }
+    grainwise_tile<kSmall>(a, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 // popcount * (1/N) of the sample masks (src/grainwise.rs:114-122), fused with the colour output:
@@ -354,22 +75,21 @@ __global__ void grainwise_epilogue_kernel(const GrainwiseEpilogueArgs a) {
     }
 }
 
-size_t grainwise_smem_bytes(const GrainwiseArgs &a) {
-    return (size_t)a.n * sizeof(float4) + (size_t)kGwWarps * kGwQueue * sizeof(float4) +
-           (size_t)kGwWarps * kGwQueue * sizeof(uint2) + (size_t)kGwWarps * kGwList * sizeof(unsigned) +
-           (size_t)a.n * sizeof(float) + ((size_t)kGwWarps * 33 + kGwBuckets + 3) * sizeof(int) +
-           (size_t)a.rmax_w * a.rmax_h * a.words * sizeof(unsigned int);
+size_t grainwise_smem_bytes(const GrainwiseArgs &a) { return grainwise_tile_smem_bytes(a); }
+
+// The directed-rounding floor/ceil needs every bounds() argument within +-2^22.
+bool grainwise_small_coords(const GrainwiseArgs &a) {
+    const float span = (float)max(a.out_w, a.out_h) +
+                       fmaxf(fmaxf(-a.offx_min, a.offx_max), fmaxf(-a.offy_min, a.offy_max)) + a.rm * a.zoom + 4.0f;
+    return span < 4194304.0f;
 }
 
 cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
     const size_t smem = grainwise_smem_bytes(a);
     dim3 grid((a.in_w + a.tin_w - 1) / a.tin_w, (a.in_h + a.tin_h - 1) / a.tin_h);
     if (grid.x == 0 || grid.y == 0) return cudaSuccess;
-    // The directed-rounding floor/ceil needs every bounds() argument within +-2^22.
-    const float span = (float)max(a.out_w, a.out_h) + fmaxf(fmaxf(-a.offx_min, a.offx_max), fmaxf(-a.offy_min, a.offy_max)) +
-                       a.rm * a.zoom + 4.0f;
     cudaError_t e;
-    if (span < 4194304.0f) {
+    if (grainwise_small_coords(a)) {
         e = cudaFuncSetAttribute(grainwise_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         grainwise_kernel<true><<<grid, kGwThreads, smem, s>>>(a);

@@ -17,7 +17,9 @@ fg_status cuda_error(cudaError_t e, const char *what);
 fg_status check_render_args(const fg_params *p, const fg_derived *d);
 bool is_device_ptr(const void *p);
 void offset_extents(const float *offs, uint32_t n, float ext[4]);
-PwPlan plan_pixelwise(const fg_params &p, const fg_derived &d, const float *h_offs_in);
+PwPlan plan_pixelwise(const fg_params &p, const fg_derived &d, const float *h_offs_in, int max_block_log2);
+PixelwiseArgs pixelwise_args(const fg_params &p, const fg_derived &d, const PwPlan &pl, const float *d_lam,
+                             const CellParam *d_cells, const float *d_offs_in, float *d_out, unsigned long long *d_diag);
 fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_derived &d, const float *h_offs_in,
                             const float *d_offs_in, float *d_out, CellParam *d_cells, unsigned long long *d_diag,
                             const EpilogueArgs *colour, cudaStream_t s);
@@ -26,7 +28,8 @@ fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_der
 size_t grain_table_bytes(uint32_t n);
 void grain_table(const float *h_offs, uint32_t n, void *blob);
 GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const float *h_offs, const float *d_lam,
-                             const void *d_table, unsigned int *d_gmask);
+                             const void *d_table, unsigned int *d_gmask, int mask_words);
+bool grainwise_small_coords(const GrainwiseArgs &a);
 size_t grainwise_mask_bytes(const fg_params &p, const fg_derived &d);
 fg_status enqueue_grainwise(const GrainwiseArgs &a, cudaStream_t s);
 fg_status enqueue_grainwise_epilogue(const GrainwiseArgs &a, float *d_out, int mode, unsigned char *d_rgb8,

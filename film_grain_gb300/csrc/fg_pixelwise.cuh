@@ -1,0 +1,437 @@
+// fg_pixelwise.cuh -- device code of the pixel-wise coverage estimator (src/pixelwise.rs:11-106),
+// shared by the standalone kernel (fg_pixelwise.cu) and the batched persistent kernel (fg_batch.cu).
+#pragma once
+#include "fg_kernels.cuh"
+#include "fg_rng.cuh"
+
+namespace fg {
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ int f2i_floor(float v) { return __float2int_rz(floorf(v)); }  // Rust `floor() as i32`
+
+__device__ __forceinline__ float xg_of(int x, float inv_zoom, float off) {
+    return FG_FSUB(FG_FMUL(FG_FADD((float)x, 0.5f), inv_zoom), off);
+}
+
+// First x in [0, n] with xg_of(x) >= X (n when none); xg_of is monotone in x.
+static __device__ int first_at_least(float X, int n, float inv_zoom, float zoom, float off) {
+    float approx = FG_FSUB(FG_FMUL(FG_FADD(X, off), zoom), 0.5f);
+    int guess;
+    if (!(approx > -8.0f)) guess = 0;
+    else if (!(approx < (float)n + 8.0f)) guess = n;
+    else guess = (int)floorf(approx);
+    int lo = max(0, guess - 3), hi = min(n, guess + 4);
+    if (lo > hi) { lo = 0; hi = n; }
+    if (lo > 0 && !(xg_of(lo - 1, inv_zoom, off) < X)) lo = 0;
+    if (hi < n && !(xg_of(hi, inv_zoom, off) >= X)) hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (xg_of(mid, inv_zoom, off) >= X) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+// mix3 (src/rng.rs:40-44) split into its column stage, shared by all cells of column i, and its
+// row stage: mix3(seed, CELL, i, j) = cell_row_hash(cell_col_hash(seed, i), j).
+__device__ __forceinline__ uint64_t cell_col_hash(unsigned long long seed, int i) {
+    return splitmix64(rotl64((seed ^ kCellStream) + (uint64_t)(int64_t)i, 17));
+}
+__device__ __forceinline__ uint64_t cell_row_hash(uint64_t col, int j) {
+    return splitmix64(rotl64(col + (uint64_t)(int64_t)j, 41));
+}
+
+// Grain count of the cell with hash h; when q > 0 the stream is left positioned after the Poisson
+// draws.  q == 0 is decided from the first draw alone: only words 0 and 3 of the seeded state enter it.
+__device__ __forceinline__ uint32_t cell_count_h(uint64_t h, long long thresh, double exp_lambda, Xoshiro &rng) {
+    uint64_t s0 = fmix64(h + kPhi), s3 = fmix64(h + 4 * kPhi);
+    uint64_t r1 = rotl64(s0 + s3, 23) + s0;
+    long long v = (long long)(r1 >> 11);
+    if (v <= thresh) return 0u;
+    rng.s0 = s0;
+    rng.s1 = fmix64(h + 2 * kPhi);
+    rng.s2 = fmix64(h + 3 * kPhi);
+    rng.s3 = s3;
+    if (thresh >= 0) {
+        (void)rng.next();  // the first draw, already evaluated
+        return poisson_knuth_tail(u53_unit((uint64_t)v), exp_lambda, rng);
+    }
+    PoissonParams P = poisson_new(-exp_lambda);
+    return poisson_rejection(P, rng);
+}
+
+// Grain count of cell (i, j); when q > 0 the stream is left positioned after the Poisson draws.
+__device__ __forceinline__ uint32_t cell_count(unsigned long long seed, int i, int j, const CellParam &cp,
+                                               Xoshiro &rng) {
+    return cell_count_h(cell_row_hash(cell_col_hash(seed, i), j), cp.thresh, cp.exp_lambda, rng);
+}
+
+__device__ __forceinline__ float radius_draw(const PixelwiseArgs &a, Xoshiro &rng) {
+    if (!a.lognorm) return a.radius_mean;
+    return lognormal_radius_f32(a.log_mu, a.log_sigma, rng);
+}
+
+__device__ __forceinline__ const CellParam &cell_param_at(const PixelwiseArgs &a, int i, int j) {
+    float sx = FG_FMUL((float)i, a.delta), sy = FG_FMUL((float)j, a.delta);
+    long long ix = (long long)floorf(sx), iy = (long long)floorf(sy);
+    ix = ix < 0 ? 0 : (ix > a.in_w - 1 ? a.in_w - 1 : ix);
+    iy = iy < 0 ? 0 : (iy > a.in_h - 1 ? a.in_h - 1 : iy);
+    return a.cells[iy * (long long)a.in_w + ix];
+}
+
+// The reference's per-sample loop (evaluate_indicator, src/pixelwise.rs:47-106), regenerating cells.
+static __device__ bool eval_regen(const PixelwiseArgs &a, const UniformF32 &U, float xg, float yg, long long i0, long long i1,
+                           long long j0, long long j1) {
+    for (long long i = i0; i <= i1; i++) {
+        for (long long j = j0; j <= j1; j++) {
+            const CellParam cp = cell_param_at(a, (int)i, (int)j);
+            Xoshiro rng;
+            uint32_t q = cell_count(a.seed, (int)i, (int)j, cp, rng);
+            if (q == 0) continue;
+            float sx = FG_FMUL((float)i, a.delta), sy = FG_FMUL((float)j, a.delta);
+            for (uint32_t g = 0; g < q; g++) {
+                float cx = FG_FADD(sx, uniform_f32_from(U, rng.next()));
+                float cy = FG_FADD(sy, uniform_f32_from(U, rng.next()));
+                float r = radius_draw(a, rng);
+                if (r > a.rm) r = a.rm;
+                if (r <= 0.0f) continue;
+                float dx = FG_FSUB(xg, cx), dy = FG_FSUB(yg, cy);
+                if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= FG_FMUL(r, r)) return true;
+            }
+        }
+    }
+    return false;
+}
+
+// Block-wide exclusive scan of one int per thread (blockDim.x == kPwThreads).
+__device__ __forceinline__ int block_excl_scan(int v, int *wsum, int *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = (lane < (kPwThreads / 32)) ? wsum[lane] : 0;
+        int t = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < (kPwThreads / 32)) wsum[lane] = t - w;
+        if (lane == (kPwThreads / 32) - 1) wsum[32] = t;
+    }
+    __syncthreads();
+    int r = wsum[warp] + x - v;
+    *total = wsum[32];
+    __syncthreads();
+    return r;
+}
+
+// ------------------------------------------------------------------ shared-memory layout
+struct PwShared {
+    float4 grains[kPwGrainMax];
+    unsigned short pre[kPwCellMax + 8];   // counts, then exclusive prefix (row-major window cells)
+    unsigned short list[kPwCellMax];      // non-empty cells
+    int colix[kPwEdgeMax], rowiy[kPwEdgeMax];
+    int4 rect[kPwKChunk];                 // owned pixel rectangle per offset: xa, xe, ya, ye
+    int spre[kPwKChunk + 1];
+    unsigned int cnt[kPwFootMax];
+    int wsum[40];
+    int stack[32][3];                     // (level, ix, iy)
+    int sp;
+    int nlist;
+    int total;
+    int flags;                            // bit0: overflow, bit1: leaf slow path
+    int fx0, fx1, fy0, fy1;               // owned-pixel footprint
+    int nsamples;
+};
+
+// One root block of the pixel-wise tile kernel (all threads of the CTA; `smem_raw` holds PwShared).
+__device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root_x, int root_y,
+                                                unsigned char *smem_raw) {
+    PwShared &S = *reinterpret_cast<PwShared *>(smem_raw);
+    const int tid = threadIdx.x;
+    const UniformF32 U = uniform_f32_new(0.0f, a.delta);
+
+    if (tid == 0) {
+        S.sp = 1;
+        S.stack[0][0] = 0; S.stack[0][1] = root_x; S.stack[0][2] = root_y;
+    }
+    __syncthreads();
+
+    while (true) {
+        __syncthreads();
+        if (S.sp == 0) break;
+        const int level = S.stack[S.sp - 1][0];
+        const int sbx = S.stack[S.sp - 1][1];
+        const int sby = S.stack[S.sp - 1][2];
+        __syncthreads();
+        if (tid == 0) S.sp--;
+        const float bs = ldexpf(a.bsize, -level);
+        const float X0 = FG_FMUL((float)sbx, bs), X1 = FG_FMUL((float)(sbx + 1), bs);
+        const float Y0 = FG_FMUL((float)sby, bs), Y1 = FG_FMUL((float)(sby + 1), bs);
+
+        // ---- ownership: rectangles per offset, sample total and pixel footprint
+        if (tid == 0) { S.fx0 = 0x7fffffff; S.fx1 = -1; S.fy0 = 0x7fffffff; S.fy1 = -1; S.nsamples = 0; }
+        __syncthreads();
+        // With N <= kPwKChunk these rectangles are kept for pass C (one chunk).
+        const bool one_chunk = a.n <= kPwKChunk;
+        {
+            int lx0 = 0x7fffffff, lx1 = -1, ly0 = 0x7fffffff, ly1 = -1, ns = 0;
+            for (int k = tid; k < a.n; k += kPwThreads) {
+                float2 o = a.offs[k];
+                int xa = first_at_least(X0, a.out_w, a.inv_zoom, a.zoom, o.x);
+                int xe = first_at_least(X1, a.out_w, a.inv_zoom, a.zoom, o.x);
+                int ya = first_at_least(Y0, a.out_h, a.inv_zoom, a.zoom, o.y);
+                int ye = first_at_least(Y1, a.out_h, a.inv_zoom, a.zoom, o.y);
+                if (one_chunk) S.rect[k] = make_int4(xa, xe, ya, ye);
+                if (xe > xa && ye > ya) {
+                    ns += (xe - xa) * (ye - ya);
+                    lx0 = min(lx0, xa); lx1 = max(lx1, xe);
+                    ly0 = min(ly0, ya); ly1 = max(ly1, ye);
+                }
+            }
+            // one shared atomic per warp instead of one per thread
+            ns = __reduce_add_sync(0xffffffffu, ns);
+            lx0 = __reduce_min_sync(0xffffffffu, lx0);
+            lx1 = __reduce_max_sync(0xffffffffu, lx1);
+            ly0 = __reduce_min_sync(0xffffffffu, ly0);
+            ly1 = __reduce_max_sync(0xffffffffu, ly1);
+            if ((tid & 31) == 0 && ns > 0) {
+                atomicAdd(&S.nsamples, ns);
+                atomicMin(&S.fx0, lx0); atomicMax(&S.fx1, lx1);
+                atomicMin(&S.fy0, ly0); atomicMax(&S.fy1, ly1);
+            }
+        }
+        __syncthreads();
+        if (S.nsamples == 0) continue;
+        const int fx0 = S.fx0, fy0 = S.fy0, fw = S.fx1 - S.fx0, fh = S.fy1 - S.fy0;
+        const bool use_cnt = (long long)fw * fh <= kPwFootMax;
+
+        // ---- staged window of cells
+        const int wi0 = f2i_floor(FG_FDIV(FG_FSUB(X0, a.rm), a.delta)) - 1;
+        const int wi1 = f2i_floor(FG_FDIV(FG_FADD(X1, a.rm), a.delta)) + 1;
+        const int wj0 = f2i_floor(FG_FDIV(FG_FSUB(Y0, a.rm), a.delta)) - 1;
+        const int wj1 = f2i_floor(FG_FDIV(FG_FADD(Y1, a.rm), a.delta)) + 1;
+        const long long Wc = (long long)wi1 - wi0 + 1, Hc = (long long)wj1 - wj0 + 1;
+        const bool window_fits = Wc > 0 && Hc > 0 && Wc <= kPwEdgeMax && Hc <= kPwEdgeMax && Wc * Hc <= kPwCellMax;
+        const int nc = window_fits ? (int)(Wc * Hc) : 0;
+
+        if (use_cnt)
+            for (int t = tid; t < fw * fh; t += kPwThreads) S.cnt[t] = 0u;
+        if (tid == 0) { S.nlist = 0; S.flags = 0; }
+        if (window_fits) {
+            for (int t = tid; t < Wc; t += kPwThreads) {
+                long long ix = (long long)floorf(FG_FMUL((float)(wi0 + t), a.delta));
+                S.colix[t] = (int)(ix < 0 ? 0 : (ix > a.in_w - 1 ? a.in_w - 1 : ix));
+            }
+            for (int t = tid; t < Hc; t += kPwThreads) {
+                long long iy = (long long)floorf(FG_FMUL((float)(wj0 + t), a.delta));
+                S.rowiy[t] = (int)(iy < 0 ? 0 : (iy > a.in_h - 1 ? a.in_h - 1 : iy));
+            }
+        }
+        __syncthreads();
+
+        bool staged = false;
+        if (window_fits) {
+            // ---- pass A: grain count per window cell.  Each thread walks a contiguous run of cells in
+            // column-major order, so the column stage of the cell hash and the lambda pixel's Poisson
+            // set-up are reused along the run; counts are stored row-major (the CSR order).
+            {
+                const int per = (nc + kPwThreads - 1) / kPwThreads;
+                const int c0 = tid * per, c1 = min(nc, c0 + per);
+                int ci = c0 / (int)Hc, cj = c0 % (int)Hc;
+                int col = -1, pix = -1;
+                uint64_t colh = 0;
+                long long thresh = 0;
+                double exp_lambda = 0.0;
+                for (int c = c0; c < c1; c++) {
+                    if (ci != col) {
+                        col = ci;
+                        colh = cell_col_hash(a.seed, wi0 + ci);
+                    }
+                    const int p = S.rowiy[cj] * a.in_w + S.colix[ci];
+                    if (p != pix) {
+                        pix = p;
+                        const CellParam cp = a.cells[p];
+                        thresh = cp.thresh;
+                        exp_lambda = cp.exp_lambda;
+                    }
+                    Xoshiro rng;
+                    const uint32_t q = cell_count_h(cell_row_hash(colh, wj0 + cj), thresh, exp_lambda, rng);
+                    const int rc = cj * (int)Wc + ci;
+                    S.pre[rc] = (unsigned short)(q > 65535u ? 65535u : q);
+                    if (q) {
+                        const int slot = atomicAdd(&S.nlist, 1);
+                        S.list[slot] = (unsigned short)rc;
+                    }
+                    if (++cj == (int)Hc) {
+                        cj = 0;
+                        ci++;
+                    }
+                }
+            }
+            __syncthreads();
+            // ---- exclusive prefix over the counts (each thread owns a contiguous run)
+            {
+                const int per = (nc + kPwThreads - 1) / kPwThreads;
+                const int b = tid * per, e = min(nc, b + per);
+                int local = 0;
+                for (int c = b; c < e; c++) local += S.pre[c];
+                int total;
+                int run = block_excl_scan(local, S.wsum, &total);
+                if (total <= kPwGrainMax) {
+                    for (int c = b; c < e; c++) {
+                        int q = S.pre[c];
+                        S.pre[c] = (unsigned short)run;
+                        run += q;
+                    }
+                }
+                if (tid == 0) {
+                    S.pre[nc] = (unsigned short)(total <= kPwGrainMax ? total : 0);
+                    S.total = total;
+                    if (total > kPwGrainMax) S.flags |= 1;
+                }
+            }
+            __syncthreads();
+            if (S.flags & 1) {
+                if (level < kPwMaxLevel) {
+                    if (tid == 0) {
+                        atomicAdd(&a.diag[2], 1ull);
+                        for (int q = 0; q < 4; q++) {
+                            int s = S.sp++;
+                            S.stack[s][0] = level + 1;
+                            S.stack[s][1] = 2 * sbx + (q & 1);
+                            S.stack[s][2] = 2 * sby + (q >> 1);
+                        }
+                    }
+                    continue;  // loop head syncs
+                }
+            } else {
+                staged = true;
+            }
+        }
+        if (!staged && tid == 0) atomicAdd(&a.diag[1], 1ull);
+
+        if (staged) {
+            // ---- pass B: regenerate the non-empty cells' grains into their CSR slots
+            const int nl = S.nlist;
+            for (int t = tid; t < nl; t += kPwThreads) {
+                const int c = S.list[t];
+                const int ci = c % (int)Wc, cj = c / (int)Wc;
+                const int i = wi0 + ci, j = wj0 + cj;
+                const CellParam cp = a.cells[(long long)S.rowiy[cj] * a.in_w + S.colix[ci]];
+                const int base = S.pre[c], end = S.pre[c + 1];  // pass A's slot range for this cell
+                uint32_t q = (uint32_t)(end - base);
+                Xoshiro rng;
+                if (cp.thresh >= 0) {
+                    // Knuth regime: the Poisson draw consumed exactly q + 1 uniforms; skip them.
+                    rng = small_seed(cell_row_hash(cell_col_hash(a.seed, i), j));
+                    for (uint32_t u = 0; u <= q; u++) (void)rng.next();
+                } else {
+                    q = min(q, cell_count(a.seed, i, j, cp, rng));
+                }
+                const float sx = FG_FMUL((float)i, a.delta), sy = FG_FMUL((float)j, a.delta);
+                for (uint32_t g = 0; g < q; g++) {
+                    float cx = FG_FADD(sx, uniform_f32_from(U, rng.next()));
+                    float cy = FG_FADD(sy, uniform_f32_from(U, rng.next()));
+                    float r = radius_draw(a, rng);
+                    if (r > a.rm) r = a.rm;
+                    float rr = (r <= 0.0f) ? -1.0f : FG_FMUL(r, r);  // -1 never passes the disk test
+                    S.grains[base + g] = make_float4(cx, cy, rr, 0.0f);
+                }
+            }
+            __syncthreads();
+        }
+
+        // ---- pass C: evaluate the owned samples, offsets in chunks
+        unsigned long long slow = 0;
+        for (int k0 = 0; k0 < a.n; k0 += kPwKChunk) {
+            const int kn = min(kPwKChunk, a.n - k0);
+            int cntk = 0;
+            if (tid < kn) {
+                int4 R;
+                if (one_chunk) {
+                    R = S.rect[tid];
+                } else {
+                    float2 o = a.offs[k0 + tid];
+                    R.x = first_at_least(X0, a.out_w, a.inv_zoom, a.zoom, o.x);
+                    R.y = first_at_least(X1, a.out_w, a.inv_zoom, a.zoom, o.x);
+                    R.z = first_at_least(Y0, a.out_h, a.inv_zoom, a.zoom, o.y);
+                    R.w = first_at_least(Y1, a.out_h, a.inv_zoom, a.zoom, o.y);
+                    S.rect[tid] = R;
+                }
+                if (R.y > R.x && R.w > R.z) cntk = (R.y - R.x) * (R.w - R.z);
+            }
+            int tot;
+            int off = block_excl_scan(tid < kPwKChunk ? cntk : 0, S.wsum, &tot);
+            if (tid < kPwKChunk) S.spre[tid] = off;
+            if (tid == 0) S.spre[kPwKChunk] = tot;
+            __syncthreads();
+            for (int s = tid; s < tot; s += kPwThreads) {
+                int lo = 0, hi = kn - 1;  // last kk with spre[kk] <= s
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (S.spre[mid] <= s) lo = mid;
+                    else hi = mid - 1;
+                }
+                const int kk = lo;
+                const int4 R = S.rect[kk];
+                const int w = R.y - R.x;
+                const int l = s - S.spre[kk];
+                const int x = R.x + l % w, y = R.z + l / w;
+                const float2 o = a.offs[k0 + kk];
+                const float xg = xg_of(x, a.inv_zoom, o.x);
+                const float yg = xg_of(y, a.inv_zoom, o.y);
+                bool hit = false;
+                if (a.rm > 0.0f) {
+                    const int i0 = f2i_floor(FG_FDIV(FG_FSUB(xg, a.rm), a.delta));
+                    const int i1 = f2i_floor(FG_FDIV(FG_FADD(xg, a.rm), a.delta));
+                    const int j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
+                    const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
+                    if (i0 <= i1 && j0 <= j1) {
+                        if (staged && i0 >= wi0 && i1 <= wi1 && j0 >= wj0 && j1 <= wj1) {
+                            const int ci0 = i0 - wi0, ci1 = i1 - wi0;
+                            for (int j = j0; j <= j1 && !hit; j++) {
+                                const int row = (j - wj0) * (int)Wc;
+                                const int gs = S.pre[row + ci0], ge = S.pre[row + ci1 + 1];
+                                for (int g = gs; g < ge; g++) {
+                                    const float4 G = S.grains[g];
+                                    const float dx = FG_FSUB(xg, G.x), dy = FG_FSUB(yg, G.y);
+                                    if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= G.z) { hit = true; break; }
+                                }
+                            }
+                        } else {
+                            slow++;
+                            hit = eval_regen(a, U, xg, yg, i0, i1, j0, j1);
+                        }
+                    }
+                }
+                if (hit) {
+                    const bool in_foot = use_cnt && x >= fx0 && x - fx0 < fw && y >= fy0 && y - fy0 < fh;
+                    if (in_foot) atomicAdd(&S.cnt[(y - fy0) * fw + (x - fx0)], 1u);
+                    else atomicAdd(&a.out[(long long)y * a.out_w + x], 1.0f);
+                }
+            }
+            __syncthreads();
+        }
+        if (slow) atomicAdd(&a.diag[0], slow);
+
+        // ---- flush per-pixel counts
+        if (use_cnt) {
+            for (int t = tid; t < fw * fh; t += kPwThreads) {
+                unsigned c = S.cnt[t];
+                if (c) atomicAdd(&a.out[(long long)(fy0 + t / fw) * a.out_w + (fx0 + t % fw)], (float)c);
+            }
+        }
+        if (tid == 0) atomicAdd(&a.diag[3], 1ull);
+    }
+}
+
+
+}  // namespace fg

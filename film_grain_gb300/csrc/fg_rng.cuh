@@ -211,17 +211,20 @@ FG_HD PoissonParams poisson_new(double lambda) {
     return p;
 }
 
-// Knuth continuation: p already holds the first uniform and exceeds exp_lambda; returns the count.
+// Knuth continuation: p already holds the first uniform and exceeds exp_lambda; returns the count
+// (the sampler's f64 `result` counter is an exact small integer, kept here as an integer).  p and
+// exp_lambda are positive doubles, whose bit patterns order like their values, so the comparison is
+// an integer one.  The draw consumes exactly count + 1 uniforms.
 template <class Rng>
 FG_HD uint32_t poisson_knuth_tail(double p, double exp_lambda, Rng &rng) {
-    double result = 2.0;  // result after the first multiplication (1 + 1)
+    const uint64_t e = f64_bits(exp_lambda);
+    uint32_t count = 1;
     p = FG_DMUL(p, std_f64_from(rng.next()));
-    while (p > exp_lambda) {
+    while (f64_bits(p) > e) {
         p = FG_DMUL(p, std_f64_from(rng.next()));
-        result = FG_DADD(result, 1.0);
+        count++;
     }
-    double r = FG_DSUB(result, 1.0);
-    return r >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)r;
+    return count;
 }
 
 // Poisson::sample, rejection branch (lambda >= 12).

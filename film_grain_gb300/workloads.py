@@ -42,3 +42,16 @@ def blobs_rgb(width: int, height: int, seed: int) -> np.ndarray:
 
 def gray_rgb(plane: np.ndarray) -> np.ndarray:
     return np.repeat(plane[:, :, None], 3, axis=2).astype(np.float32)
+
+
+def batched_sweep(n_images: int = 64, seed: int = 7, sizes=(128, 256, 512, 1024, 2048),
+                  radii=(0.025, 0.05, 0.1, 0.2), samples=(16, 64, 256)):
+    """The uneven batch: n luma images of the blob family, each with a seeded size (square, uniform over
+    `sizes`), constant grain radius (uniform over `radii`), N (uniform over `samples`) and image seed.
+    Returns a list of dicts (size, radius, n, seed, image_seed)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_images):
+        out.append(dict(size=int(rng.choice(sizes)), radius=float(rng.choice(radii)), n=int(rng.choice(samples)),
+                        seed=int(rng.integers(0, 2**32)), image_seed=1000 + k))
+    return out

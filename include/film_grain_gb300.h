@@ -197,6 +197,43 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
 FG_API fg_status fg_dry_run(int64_t width, int64_t height, const fg_params *params, fg_render_stats *stats);
 
 /* ---------------------------------------------------------------------------------------------
+ * Batches: many images of uneven sizes and parameters in one persistent launch behind a CUDA graph.
+ * No counterpart in the crate (which renders one image per call); results equal the per-image
+ * fg_render_pixelwise / fg_render_grainwise outputs bit for bit.
+ * ------------------------------------------------------------------------------------------- */
+
+typedef struct fg_batch_image {
+    int32_t algo;                  /* FG_ALGO_PIXEL or FG_ALGO_GRAIN (resolved, e.g. by fg_choose_algorithm) */
+    const fg_params *params;       /* read at fg_batch_create */
+    const fg_derived *derived;     /* read at fg_batch_create */
+    const float *offsets;          /* host [n][2]: offsets_input for pixel-wise, offsets for grain-wise */
+    const float *d_lambda;         /* device, input_width x input_height (read at every run) */
+    float *d_out;                  /* device, output_width x output_height (written at every run) */
+    const float *h_lambda;         /* optional host copy of lambda, used only to estimate tile costs */
+} fg_batch_image;
+
+typedef struct fg_batch_tuning {
+    int32_t grain_mask_words;      /* shared-memory mask words per grain-wise tile (sets the tile edge) */
+    int32_t pixel_max_block_log2;  /* largest pixel-wise block edge, log2 of input pixels */
+    int32_t ctas_per_sm;           /* persistent CTAs per SM */
+} fg_batch_tuning;
+
+typedef struct fg_batch fg_batch;
+
+/* Plans the images, allocates the batch's scratch, uploads the work list and captures the graph.
+ * tuning may be NULL (defaults).  Synchronous. */
+FG_API fg_status fg_batch_create(const fg_batch_image *images, int32_t n_images, const fg_batch_tuning *tuning,
+                                 fg_batch **out);
+/* Replays the graph on `stream` (asynchronous): every image's d_out is rendered from its d_lambda. */
+FG_API fg_status fg_batch_run(fg_batch *batch, void *stream);
+FG_API fg_status fg_batch_destroy(fg_batch *batch);
+FG_API fg_status fg_batch_get_tuning(const fg_batch *batch, fg_batch_tuning *out);
+/* Times candidate tunings on these images (creating and running a batch for each) and returns the
+ * fastest, with its graph time in milliseconds when best_ms is not NULL.  Synchronous. */
+FG_API fg_status fg_batch_autotune(const fg_batch_image *images, int32_t n_images, void *stream,
+                                   fg_batch_tuning *best, float *best_ms);
+
+/* ---------------------------------------------------------------------------------------------
  * Diagnostics.
  * ------------------------------------------------------------------------------------------- */
 
