@@ -192,6 +192,92 @@ def grainwise_lane_ops(count, wl, out_px):
                  GW_COST["hit"] * count["hits_per_grain"]) + out_px * (GW_COST["out_base"] + GW_COST["out_word"] * words))
 
 
+def run_batch(args, rank, world):
+    """The uneven sweep: 64 luma images (blob family), sizes over {128..2048}^2, radius over
+    {0.025..0.2}, N over {16, 64, 256}, algorithm chosen per image by the crate's Auto rule.  value =
+    all images' samples / the autotuned batched graph's time; the per-image launch time is reported."""
+    import torch
+    import film_grain_gb300 as fg
+    from film_grain_gb300 import build as fgbuild, workloads
+    fgbuild.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    L = fg.lib()
+    specs = workloads.batched_sweep(64, seed=7)
+    images, host_lam, samples = [], [], 0
+    for sp in specs:
+        plane = workloads.blobs_plane(sp["size"], sp["size"], sp["image_seed"])
+        p = fg.ParamsBuilder(radius_mean=sp["radius"], n_samples=sp["n"], seed=sp["seed"]).build()
+        d = fg.derive_common(p, (sp["size"], sp["size"]))
+        lam = fg.lambda_plane(fg.normalize_plane(plane)[0], d.inv_e_pi_r2)
+        algo = fg.choose_algorithm(p, d)
+        images.append((torch.from_numpy(lam).cuda(), p, d, algo, lam))
+        host_lam.append(lam)
+        samples += d.output_width * d.output_height * sp["n"]
+    stream = torch.cuda.current_stream()
+    sp_ = stream.cuda_stream
+    outs = [torch.empty((im[2].output_height, im[2].output_width), device="cuda") for im in images]
+    offs = [np.ascontiguousarray(im[2].offsets_input if im[3] == fg.Algo.Pixel else im[2].offsets, np.float32)
+            for im in images]
+
+    def per_image():
+        for (lam, p, d, algo, _), o, of in zip(images, outs, offs):
+            fn = L.fg_render_pixelwise_async if algo == fg.Algo.Pixel else L.fg_render_grainwise_async
+            if fn(lam.data_ptr(), p.c, d._c, of.ctypes.data, o.data_ptr(), sp_) != 0:
+                raise RuntimeError(L.fg_last_error_message().decode())
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    t_per_image = timed(per_image, args.steps, args.warmup)
+    b_default = fg.Batch(images)
+    t_default = timed(b_default.run, args.steps, args.warmup)
+    b_default.close()
+    best, t_tune = fg.Batch.autotune(images)
+    b = fg.Batch(images, best)
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    t_batch = timed(b.run, args.steps, args.warmup)
+    clk = clocks.stop()
+    # end to end: pinned lambda planes in, f32 planes out, around the batched graph
+    pin_in = [torch.from_numpy(h).pin_memory() for h in host_lam]
+    pin_out = [torch.empty(o.shape, dtype=torch.float32).pin_memory() for o in b.outputs]
+
+    def e2e():
+        for (lam, *_), pi in zip(images, pin_in):
+            lam.copy_(pi, non_blocking=True)
+        b.run()
+        for o, po in zip(b.outputs, pin_out):
+            po.copy_(o, non_blocking=True)
+    t_e2e = timed(e2e, args.steps, args.warmup)
+    h2d = sum(h.nbytes for h in host_lam)
+    d2h = sum(o.numel() * 4 for o in b.outputs)
+    line = {"metric": "MC samples/s", "value": samples / (t_batch / 1e3), "unit": "samples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batch, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64-rng/f32", "data": "synthetic (seeded)",
+            "config": {"workload": "batch_sweep_64", "images": len(images),
+                       "pixel_images": sum(1 for im in images if im[3] == fg.Algo.Pixel),
+                       "frame_samples": samples, "per_image_launch_ms": t_per_image,
+                       "batched_default_ms": t_default, "batched_autotuned_ms": t_batch,
+                       "speedup_vs_per_image": t_per_image / t_batch, "tuning": repr(best),
+                       "autotune_best_ms": t_tune, "l2": "inputs and scratch far larger than L2"},
+            "e2e": {"value": samples / (t_e2e / 1e3), "unit": "samples/s", "ms_per_step": t_e2e,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "path": "pinned lambda planes -> fg_batch_run -> pinned f32 planes"},
+            "gpu_launches": 3 * args.steps, "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    b.close()
+
+
 def run_reference(args, wl, rank):
     import oracle
     if rank != 0:
@@ -226,12 +312,19 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="grain_rgb_1024", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="grain_rgb_1024", choices=sorted(WORKLOADS) + ["batch_sweep_64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-once", action="store_true",
                     help="render plane 0 once after one warm-up render and exit (a small case for ncu captures)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.workload == "batch_sweep_64":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batched sweep has no reference counterpart"}))
+            return
+        run_batch(args, int(os.environ.get("RANK", "0")), world)
+        return
     wl = WORKLOADS[args.workload]
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

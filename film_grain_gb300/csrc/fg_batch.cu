@@ -359,8 +359,8 @@ FG_API fg_status fg_batch_autotune(const fg_batch_image *images, int32_t n_image
     if (!images || n_images <= 0 || !best) return set_error(FG_ERR_INVALID, "empty batch");
     cudaStream_t s = (cudaStream_t)stream;
     const int masks[] = {16384, 8192};
-    const int blocks[] = {4, 3, 2};
-    const int ctas[] = {2, 1};
+    const int blocks[] = {4, 2};
+    const int ctas[] = {2};
     float best_t = 1e30f;
     fg_batch_tuning best_cfg = default_tuning();
     cudaEvent_t e0, e1;
