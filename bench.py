@@ -192,6 +192,174 @@ def grainwise_lane_ops(count, wl, out_px):
                  GW_COST["hit"] * count["hits_per_grain"]) + out_px * (GW_COST["out_base"] + GW_COST["out_word"] * words))
 
 
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def surrogate_compare(fg, sg, net, steps, warmup, plain_steps, clocks=None, seed=7):
+    """The large frame (4096^2 x 3 blob family, lognormal r 0.025/0.01, sigma 0.8): the surrogate's
+    ms/frame against the plain pixel-wise render at N=256, both on device-resident inputs with a 256 MiB
+    L2 flush before every frame, and both scored (MAE, spectrum error) against a plain render at N=1024
+    with another seed.  Returns a dict of the measurements."""
+    import torch
+    from film_grain_gb300 import workloads
+    wl = WORKLOADS["pixel_rgb_4096"]
+    size = wl["w"]
+    planes = host_planes(workloads.blobs_rgb(size, size, wl["image_seed"]), "rgb")
+    u_host = np.stack([fg.normalize_plane(p)[0] for p in planes])
+    u_dev = torch.from_numpy(u_host).cuda()
+    radius = torch.full((3,), wl["radius"], dtype=torch.float32, device="cuda")
+    y = torch.empty_like(u_dev)
+    L = fg.lib()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def plain(n_samples, pseed, out):
+        p = fg.ParamsBuilder(radius_mean=wl["radius"], radius_dist=fg.RadiusDist.Lognorm, radius_stddev=wl["sd"],
+                             n_samples=n_samples, seed=pseed, algo=fg.Algo.Pixel).build()
+        d = fg.derive_common(p, (size, size))
+        lam = [torch.from_numpy(fg.lambda_plane(u_host[c], d.inv_e_pi_r2)).cuda() for c in range(3)]
+        offs = np.ascontiguousarray(d.offsets_input, np.float32)
+
+        def run():
+            for c in range(3):
+                rc = L.fg_render_pixelwise_async(lam[c].data_ptr(), p.c, d._c, offs.ctypes.data, out[c].data_ptr(), sp)
+                if rc != 0:
+                    raise RuntimeError(L.fg_last_error_message().decode())
+        return run
+
+    def timed(fn, k):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        for e0, e1 in evs:
+            flush.fill_(1.0)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return sum(e0.elapsed_time(e1) for e0, e1 in evs) / k
+
+    sur = lambda: net.infer(u_dev, radius, seed=seed, out=y)
+    plain256 = torch.empty_like(u_dev)
+    run256 = plain(256, wl["seed"], plain256)
+    for _ in range(warmup):
+        sur()
+    run256()
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+    sur_ms = timed(sur, steps)
+    clk = clocks.stop() if clocks else None
+    plain_ms = timed(run256, plain_steps)
+
+    # the dominant kernel: the 32 -> 32 residual conv, timed per launch through the layer-by-layer path
+    ws = net._workspace(3, size, size, train=False)
+    net.forward(u_dev, radius, seed=seed)
+    hs = ws["hs"]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(net.n_res)]
+    for l, (e0, e1) in enumerate(evs):
+        e0.record(stream)
+        net._conv(sg.CONV_RESIDUAL, hs[l % 2], sg.CH, net._ptr(net.wbf, "w_res", l), net._ptr(net.w32, "b_res", l),
+                  hs[l % 2], None, hs[(l + 1) % 2], None, None, 3, size, size)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    conv_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / len(evs)
+    px = 3 * size * size
+    conv_flop = px * 9 * sg.CH * sg.CH * 2
+    conv_bytes = px * sg.CH * 2 * 3  # read h, read the residual, write h'
+
+    judge = torch.empty_like(u_dev)
+    plain(1024, wl["seed"] + 1000, judge)()
+    # the method without the network at the network's cost: plain pixel-wise with N scaled to its time
+    n_eq = max(1, int(round(256 * sur_ms / plain_ms)))
+    plain_eq = torch.empty_like(u_dev)
+    plain(n_eq, wl["seed"], plain_eq)()
+    torch.cuda.synchronize()
+    q_sur = sg.evaluate(y, judge)
+    q_plain = sg.evaluate(plain256, judge)
+    q_eq = dict(sg.evaluate(plain_eq, judge), n_samples=n_eq)
+    q_id = sg.evaluate(u_dev, judge)
+
+    # end to end: pinned host u planes in, pinned host f32 planes out
+    pin_u = torch.from_numpy(u_host).pin_memory()
+    pin_y = torch.empty_like(pin_u).pin_memory()
+    u_e2e = torch.empty_like(u_dev)
+
+    def e2e():
+        u_e2e.copy_(pin_u, non_blocking=True)
+        net.infer(u_e2e, radius, seed=seed, out=y)
+        pin_y.copy_(y, non_blocking=True)
+    for _ in range(warmup):
+        e2e()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        e2e()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+    return dict(size=size, sur_ms=sur_ms, plain_ms=plain_ms, conv_ms=conv_ms, conv_flop=conv_flop,
+                conv_bytes=conv_bytes, q_sur=q_sur, q_plain=q_plain, q_eq=q_eq, q_id=q_id, e2e_ms=e2e_ms,
+                h2d=4 * px, d2h=4 * px, clocks=clk, launches_per_frame=3 + net.n_res, wl=wl, planes=planes)
+
+
+def run_surrogate(args, rank, world):
+    """--workload surrogate_rgb_4096: the surrogate against the plain method on the large frame."""
+    import torch
+    import film_grain_gb300 as fg
+    from film_grain_gb300 import build as fgbuild
+    from film_grain_gb300 import surrogate as sg
+    fgbuild.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if args.retrain or not os.path.exists(sg.DEFAULT_WEIGHTS):
+        net, info = sg.train_from_scratch(log=log)
+        prov = dict(source="trained in this run", **info)
+    else:
+        net = sg.load_default()
+        prov = dict(source="film_grain_gb300/weights/surrogate_c4.npz", **{k: (v.item() if hasattr(v, "item") else v)
+                                                                           for k, v in net.meta.items()})
+    clocks = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    r = surrogate_compare(fg, sg, net, args.steps, args.warmup, plain_steps=min(args.steps, 3), clocks=clocks)
+    if rank != 0:
+        return
+    peaks, basis = _peaks()
+    ach = r["conv_flop"] / (r["conv_ms"] / 1e3) / 1e12
+    line = {"metric": "surrogate ms/frame (4096^2 RGB)", "value": r["sur_ms"], "unit": "ms/frame", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["sur_ms"], "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (f32 accumulate)",
+            "data": "synthetic (seeded blob frame)",
+            "config": {"workload": "surrogate_rgb_4096",
+                       "description": "4096x4096x3 blob frame, lognormal r 0.025/0.01, sigma 0.8, zoom 1: "
+                                      "surrogate vs plain pixel-wise N=256, scored against plain N=1024",
+                       "plain_ms_per_frame": r["plain_ms"], "speedup_vs_plain": r["plain_ms"] / r["sur_ms"],
+                       "l2": "256 MiB flush write before every frame", "network": prov},
+            "quality": {"surrogate_vs_n1024": r["q_sur"], "plain_n256_vs_n1024": r["q_plain"],
+                        "plain_equal_time_vs_n1024": r["q_eq"], "identity_vs_n1024": r["q_id"],
+                        "targets": {"mae": 0.01, "raps": 0.02}},
+            "roofline": {"bound": "tensor", "achieved": ach, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                         "frac": ach / peaks["bf16_tflops"], "traffic": None,
+                         "kernel": "sg_conv_fwd<32,32,residual>", "launch_ms": r["conv_ms"],
+                         "flop_per_launch": r["conv_flop"], "algorithmic_bytes_per_launch": r["conv_bytes"],
+                         "hbm_frac": r["conv_bytes"] / (r["conv_ms"] / 1e3) / (peaks["hbm_gbs"] * 1e9),
+                         "peak_basis": f"bf16 burst, {basis}"},
+            "e2e": {"value": r["e2e_ms"], "unit": "ms/frame", "h2d_bytes_per_step": r["h2d"] + 12,
+                    "d2h_bytes_per_step": r["d2h"], "path": "pinned f32 u planes -> fg_sg_infer -> pinned f32 planes"},
+            "gpu_launches": args.steps * r["launches_per_frame"], "clocks": r["clocks"]}
+    if not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        threads = os.cpu_count() or 1
+        rate, secs, desc, _ = cpu_pixel_baseline(oracle, r["planes"], r["wl"], threads, rows=2)
+        frame = 3 * r["size"] * r["size"] * r["wl"]["n"]
+        line["cpu_baseline"] = {"value": frame / rate * 1e3, "unit": "ms/frame", "cores": threads, "kind": "port",
+                                "sample": f"plain pixel-wise N=256 oracle on {desc}, extrapolated to the frame",
+                                "seconds": secs}
+    print(json.dumps(line), flush=True)
+
+
 def run_batch(args, rank, world):
     """The uneven sweep: 64 luma images (blob family), sizes over {128..2048}^2, radius over
     {0.025..0.2}, N over {16, 64, 256}, algorithm chosen per image by the crate's Auto rule.  value =
@@ -312,7 +480,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="grain_rgb_1024", choices=sorted(WORKLOADS) + ["batch_sweep_64"])
+    ap.add_argument("--workload", default="grain_rgb_1024",
+                    choices=sorted(WORKLOADS) + ["batch_sweep_64", "surrogate_rgb_4096"])
+    ap.add_argument("--retrain", action="store_true",
+                    help="surrogate_rgb_4096: train the network in this run instead of loading the shipped weights")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-once", action="store_true",
                     help="render plane 0 once after one warm-up render and exit (a small case for ncu captures)")
@@ -324,6 +495,12 @@ def main():
             print(json.dumps({"impl": "reference", "unavailable": "the batched sweep has no reference counterpart"}))
             return
         run_batch(args, int(os.environ.get("RANK", "0")), world)
+        return
+    if args.workload == "surrogate_rgb_4096":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the surrogate has no reference counterpart"}))
+            return
+        run_surrogate(args, int(os.environ.get("RANK", "0")), world)
         return
     wl = WORKLOADS[args.workload]
 

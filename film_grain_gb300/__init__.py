@@ -141,6 +141,12 @@ class _BatchImageC(ctypes.Structure):
                 ("h_lambda", ctypes.c_void_p)]
 
 
+class _SgNetC(ctypes.Structure):
+    _fields_ = [("n_res", ctypes.c_int32), ("radius_scale", ctypes.c_float), ("w_in", ctypes.c_void_p),
+                ("b_in", ctypes.c_void_p), ("w_res", ctypes.c_void_p), ("b_res", ctypes.c_void_p),
+                ("w_out", ctypes.c_void_p), ("b_out", ctypes.c_void_p)]
+
+
 class BatchTuning(ctypes.Structure):
     """fg_batch_tuning: grain-wise tile mask budget, pixel-wise block edge, persistent CTAs per SM."""
     _fields_ = [("grain_mask_words", ctypes.c_int32), ("pixel_max_block_log2", ctypes.c_int32),
@@ -179,6 +185,22 @@ SIGNATURES = {
     "fg_batch_get_tuning": (ctypes.c_int, [ctypes.c_void_p, _P(BatchTuning)]),
     "fg_batch_autotune": (ctypes.c_int, [_P(_BatchImageC), ctypes.c_int32, _vp, _P(BatchTuning),
                                          _P(ctypes.c_float)]),
+    "fg_sg_conv_forward": (ctypes.c_int, [ctypes.c_int32, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                          ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _vp]),
+    "fg_sg_conv_wgrad": (ctypes.c_int, [ctypes.c_int32, _vp, ctypes.c_int32, _vp, ctypes.c_int32, _vp, _vp,
+                                        ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _vp]),
+    "fg_sg_mask_grad": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int64, _vp]),
+    "fg_sg_flip_weights": (ctypes.c_int, [_vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                          _vp]),
+    "fg_sg_adam": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_int64,
+                                  ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_int32,
+                                  _vp]),
+    "fg_sg_make_input": (ctypes.c_int, [_vp, _vp, ctypes.c_float, ctypes.c_uint64, _vp, ctypes.c_int32,
+                                        ctypes.c_int32, ctypes.c_int32, _vp]),
+    "fg_sg_mse_grad": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int64, ctypes.c_float, _vp]),
+    "fg_sg_infer_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "fg_sg_infer": (ctypes.c_int, [_P(_SgNetC), _vp, _vp, ctypes.c_uint64, _vp, ctypes.c_int32, ctypes.c_int32,
+                                   ctypes.c_int32, _vp, ctypes.c_size_t, _vp]),
 }
 
 _lib: Optional[ctypes.CDLL] = None

@@ -234,6 +234,73 @@ FG_API fg_status fg_batch_autotune(const fg_batch_image *images, int32_t n_image
                                    fg_batch_tuning *best, float *best_ms);
 
 /* ---------------------------------------------------------------------------------------------
+ * Surrogate: a residual 3x3-conv network that predicts the rendered plane from the normalised
+ * intensity u, a seeded N(0,1) noise field and the grain radius.  No counterpart in the crate: it
+ * stands in for the MC integrators in interactive previews, while fg_render_* remain the method of
+ * record.  Layout: activations NHWC bf16 (channel stride 16 or 32), weights [cout][9 taps][cin] bf16
+ * with tap = 3*ky + kx, biases f32.  Every pointer is device memory; every call is asynchronous on
+ * `stream`.  Network:
+ *   x   = (u, noise, radius * radius_scale, 0 ...)          16 channels
+ *   h0  = relu(conv_in(x) + b_in)                          w_in  [32][9][16]
+ *   h_l = h_{l-1} + relu(conv_l(h_{l-1}) + b_l)            w_res [n_res][32][9][32]
+ *   y   = u + conv_out(h_L)[channel 0] + b_out[0]          w_out [8][9][32] (rows 1..7 zero)
+ * ------------------------------------------------------------------------------------------- */
+
+enum {
+    FG_SG_CONV_INPUT = 0,           /* 16 -> 32, out = relu(z + b) */
+    FG_SG_CONV_RESIDUAL = 1,        /* 32 -> 32, out = res + relu(z + b); aux (if not NULL) = relu(z + b) */
+    FG_SG_CONV_OUTPUT = 2,          /* 32 -> 8, out_f32 = res_f32 + z[0] + b[0] */
+    FG_SG_CONV_DGRAD_RESIDUAL = 3,  /* 32 -> 32, out = res + z (no bias): data gradient of a residual conv */
+    FG_SG_CONV_DGRAD_OUTPUT = 4     /* 16 -> 32, out = z (no bias): data gradient of the output conv */
+};
+
+typedef struct fg_sg_net {
+    int32_t n_res;                 /* residual layers */
+    float radius_scale;            /* radius input channel = radius * radius_scale */
+    const void *w_in;              /* bf16 [32][9][16] */
+    const float *b_in;             /* [32] */
+    const void *w_res;             /* bf16 [n_res][32][9][32] */
+    const float *b_res;            /* [n_res][32] */
+    const void *w_out;             /* bf16 [8][9][32] */
+    const float *b_out;            /* [8] */
+} fg_sg_net;
+
+/* One 3x3 conv over nb images of height x width (kind above; in_cstride = input channel stride, a
+ * multiple of 8 and at least the kind's input channels; in and w 16-byte aligned). */
+FG_API fg_status fg_sg_conv_forward(int32_t kind, const void *in, int32_t in_cstride, const void *w, const float *bias,
+                                    const void *res, const float *res_f32, void *out, void *aux, float *out_f32,
+                                    int32_t nb, int32_t height, int32_t width, void *stream);
+/* Adds the weight and bias gradients of a forward conv of `kind` (INPUT, RESIDUAL or OUTPUT) into the
+ * f32 buffers dw [cout][9][cin] and db [cout]: gout is the gradient at the conv output (before the
+ * bias, channel stride g_cstride), x the conv input (channel stride x_cstride). */
+FG_API fg_status fg_sg_conv_wgrad(int32_t kind, const void *gout, int32_t g_cstride, const void *x, int32_t x_cstride,
+                                  float *dw, float *db, int32_t nb, int32_t height, int32_t width, void *stream);
+/* g[i] = relu[i] > 0 ? dh[i] : 0 over n bf16 elements. */
+FG_API fg_status fg_sg_mask_grad(const void *dh, const void *relu, void *g, int64_t n, void *stream);
+/* wt[ci][8 - tap][co] = w[co][tap][ci] (zero in the padding), the weights of the data-gradient conv. */
+FG_API fg_status fg_sg_flip_weights(const void *w, void *wt, int32_t cout, int32_t cin, int32_t cout_pad,
+                                    int32_t cin_pad, void *stream);
+/* One Adam step (bias-corrected with `step` >= 1) on f32 weights w with moments m, v and decoupled
+ * weight decay w -= lr * decay[i] * w (decay may be NULL: none); also writes the bf16 copy w_bf16 when
+ * it is not NULL, and the weight average ema = ema_decay * ema + (1 - ema_decay) * w when ema is not NULL. */
+FG_API fg_status fg_sg_adam(float *w, float *m, float *v, const float *grad, const float *decay, void *w_bf16,
+                            float *ema, float ema_decay, int64_t n, float lr, float beta1, float beta2, float eps,
+                            int32_t step, void *stream);
+/* Builds the 16-channel network input from u [nb][h][w] and one radius per image; the noise field is
+ * a function of (seed, pixel index in the batch) only. */
+FG_API fg_status fg_sg_make_input(const float *u, const float *radius, float radius_scale, uint64_t seed, void *x,
+                                  int32_t nb, int32_t height, int32_t width, void *stream);
+/* dy16[p] = (scale * (y[p] - target[p]), 0 x 15) in bf16, and *loss_sum += sum (y - target)^2. */
+FG_API fg_status fg_sg_mse_grad(const float *y, const float *target, void *dy16, float *loss_sum, int64_t n,
+                                float scale, void *stream);
+/* Scratch needed by fg_sg_infer. */
+FG_API size_t fg_sg_infer_workspace_bytes(int32_t nb, int32_t height, int32_t width);
+/* The whole network forward: out [nb][h][w] f32 from u [nb][h][w] and radius [nb]. */
+FG_API fg_status fg_sg_infer(const fg_sg_net *net, const float *u, const float *radius, uint64_t seed, float *out,
+                             int32_t nb, int32_t height, int32_t width, void *workspace, size_t workspace_bytes,
+                             void *stream);
+
+/* ---------------------------------------------------------------------------------------------
  * Diagnostics.
  * ------------------------------------------------------------------------------------------- */
 
