@@ -180,6 +180,12 @@ def cpu_pixel_baseline(oracle, planes, wl, threads, rows=None):
     return samples / dt, dt, f"output rows {y0}..{y0 + r} of plane 0 ({samples} samples)", None
 
 
+# DRAM bytes per launch measured by ncu on the profiling cases (profiles/*_ncu.md), per unit of work:
+# sg_conv_fwd<32,32,residual>: 354.6 MB read+write for 3 x 1024^2 px; grainwise_kernel: 17.94 MB for a
+# 1024^2-pixel output plane (the lambda plane plus the sample-mask lines that miss L2).
+SG_CONV_DRAM_BYTES_PER_PX = 354.6e6 / (3 * 1024 * 1024)
+GRAINWISE_DRAM_BYTES_PER_OUT_PX = 17.94e6 / (1024 * 1024)
+
 # Algorithmic lane-ops of the grain-wise path (minimal exact implementation; derivation in the design doc).
 GW_COST = dict(grain_lognorm=150, grain_const=70, x_pair=10, y_pair=8, hit=12, out_base=3, out_word=2)
 
@@ -270,7 +276,7 @@ def surrogate_compare(fg, sg, net, steps, warmup, plain_steps, clocks=None, seed
     conv_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / len(evs)
     px = 3 * size * size
     conv_flop = px * 9 * sg.CH * sg.CH * 2
-    conv_bytes = px * sg.CH * 2 * 3  # read h, read the residual, write h'
+    conv_bytes = px * sg.CH * 2 * 2  # read h (the residual is the same tensor), write h'
 
     judge = torch.empty_like(u_dev)
     plain(1024, wl["seed"] + 1000, judge)()
@@ -314,6 +320,17 @@ def run_surrogate(args, rank, world):
     from film_grain_gb300 import surrogate as sg
     fgbuild.build()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if args.profile_once:  # small case for ncu: the shipped network on a 1024^2 x 3 blob frame, twice
+        from film_grain_gb300 import workloads
+        net = sg.load_default()
+        planes = host_planes(workloads.blobs_rgb(1024, 1024, 1), "rgb")
+        u = torch.from_numpy(np.stack([fg.normalize_plane(p)[0] for p in planes])).cuda()
+        radius = torch.full((3,), 0.025, dtype=torch.float32, device="cuda")
+        for _ in range(2):
+            net.infer(u, radius, seed=7)
+        torch.cuda.synchronize()
+        log("profile-once: surrogate on 1024^2 x 3 rendered twice")
+        return
     if args.retrain or not os.path.exists(sg.DEFAULT_WEIGHTS):
         net, info = sg.train_from_scratch(log=log)
         prov = dict(source="trained in this run", **info)
@@ -340,7 +357,10 @@ def run_surrogate(args, rank, world):
                         "plain_equal_time_vs_n1024": r["q_eq"], "identity_vs_n1024": r["q_id"],
                         "targets": {"mae": 0.01, "raps": 0.02}},
             "roofline": {"bound": "tensor", "achieved": ach, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-                         "frac": ach / peaks["bf16_tflops"], "traffic": None,
+                         "frac": ach / peaks["bf16_tflops"],
+                         "traffic": SG_CONV_DRAM_BYTES_PER_PX * 3 * r["size"] ** 2,
+                         "traffic_basis": "ncu dram bytes of one 3x1024^2 launch "
+                                          "(profiles/sg_conv_fwd_surrogate_1024_ncu.md), scaled by pixels",
                          "kernel": "sg_conv_fwd<32,32,residual>", "launch_ms": r["conv_ms"],
                          "flop_per_launch": r["conv_flop"], "algorithmic_bytes_per_launch": r["conv_bytes"],
                          "hbm_frac": r["conv_bytes"] / (r["conv_ms"] / 1e3) / (peaks["hbm_gbs"] * 1e9),
@@ -647,7 +667,9 @@ def main():
         ops = [grainwise_lane_ops(c, wl, ow * oh) for c in counts]
         ach = sum(o / (ms / 1e3) for o, ms in zip(ops, launch_ms)) / len(ops)
         line["roofline"] = {"bound": "sm_issue", "achieved": ach / 1e12, "peak": peak / 1e12, "unit": "Tlane-op/s",
-                            "frac": ach / peak, "traffic": None,
+                            "frac": ach / peak, "traffic": GRAINWISE_DRAM_BYTES_PER_OUT_PX * ow * oh,
+                            "traffic_basis": "ncu dram bytes of the grain_rgb_512 launch "
+                                             "(profiles/grainwise_kernel_grain_rgb_512_ncu.md), scaled by output pixels",
                             "kernel": "grainwise_kernel", "launch_ms": launch_ms,
                             "lane_ops_per_launch": ops, "counts": counts,
                             "peak_basis": f"{sm_count} SMs x 128 lanes x {f_mhz:.0f} MHz (sampled)"}
