@@ -13,12 +13,14 @@
 //   - each warp takes 32 footprint pixels at a time (one per lane, Poisson set-up in step) and
 //     draws their grains one per lane per step; valid grains are compacted into a 64-entry warp
 //     queue with a ballot, and every full batch of 32 is rasterised grain by grain by the whole warp;
-//   - the offsets are sorted by the fractional part of their x component.  An offset can put a
-//     pixel centre inside a grain's disk only if frac(czx + offx) lies within radius_out of 1/2
-//     (and likewise for y), so only the cyclic interval of the sorted table around frac(1/2 - czx),
-//     widened by a rounding margin, is examined: stage A flattens those (grain, offset) pairs over
-//     the lanes and filters them by the same test on the y fractions; stage B runs the reference's
-//     exact bounds() and centre tests on the compacted survivors, one pair per lane;
+//   - an offset can put a pixel centre inside a grain's disk only if frac(czx + offx) lies within
+//     radius_out of 1/2 (and likewise for y).  For N <= 256 each lane turns both tests, widened by a
+//     rounding margin and rounded out to 1/64 buckets, into a bitmask over the sample index (two
+//     lookups per axis in per-tile sparse OR tables), ANDs them, and the set bits -- about 1.2x the
+//     true candidates -- go through the warp's list to stage B.  For larger N the offsets are sorted
+//     by frac(offx), the cyclic interval of the sorted table around frac(1/2 - czx) is flattened over
+//     the lanes (stage A) and filtered by the y test.  Stage B runs the reference's exact bounds()
+//     and centre tests on the pairs, one pair per lane;
 //   - the lognormal radius is evaluated with the double-float exp (exp_f64_to_f32).
 // Bits are set with shared-memory atomicOr; OR is idempotent and commutative, so the result does not
 // depend on the order.
@@ -30,10 +32,10 @@
 
 namespace fg {
 
-template <bool kSmall>
+template <bool kSmall, int kVariant>
 __global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const __grid_constant__ GrainwiseArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    grainwise_tile<kSmall>(a, blockIdx.x, blockIdx.y, smem_raw);
+    grainwise_tile<kSmall, kVariant>(a, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 // popcount * (1/N) of the sample masks (src/grainwise.rs:114-122), fused with the colour output:
@@ -88,16 +90,14 @@ cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
     const size_t smem = grainwise_smem_bytes(a);
     dim3 grid((a.in_w + a.tin_w - 1) / a.tin_w, (a.in_h + a.tin_h - 1) / a.tin_h);
     if (grid.x == 0 || grid.y == 0) return cudaSuccess;
-    cudaError_t e;
-    if (grainwise_small_coords(a)) {
-        e = cudaFuncSetAttribute(grainwise_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        grainwise_kernel<true><<<grid, kGwThreads, smem, s>>>(a);
-    } else {
-        e = cudaFuncSetAttribute(grainwise_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        grainwise_kernel<false><<<grid, kGwThreads, smem, s>>>(a);
-    }
+    const bool small = grainwise_small_coords(a);
+    const int v = grainwise_variant(a.n);
+    void (*k)(GrainwiseArgs);
+    if (small) k = v == 4 ? grainwise_kernel<true, 4> : (v == 8 ? grainwise_kernel<true, 8> : grainwise_kernel<true, 0>);
+    else k = v == 4 ? grainwise_kernel<false, 4> : (v == 8 ? grainwise_kernel<false, 8> : grainwise_kernel<false, 0>);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, kGwThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -173,10 +173,244 @@ __device__ __forceinline__ void gw_raster_batch(const GwTile &T, unsigned int *m
     gw_drain<kSmall>(T, mask, tab, q, list, ln, lane);
 }
 
-// One input tile of the grain-wise kernel (all threads of the CTA; `smem_raw` holds its shared memory).
+// ------------------------------------------------------------------ bitmask candidate filter (N <= 256)
+// For N <= 256 the candidate offsets of a grain are found as a bitmask over the sample index k: the
+// unit interval of frac(offset) is cut into 64 buckets, and for each axis a sparse table holds, for
+// every bucket b and level L, the OR of the sample masks of buckets b .. b + 2^L - 1 (cyclic).  The
+// cyclic interval [c - h, c + h] of an axis test, rounded out to whole buckets, is the OR of two table
+// entries; the AND of the x and y masks is a superset of the pairs that pass both of the tests the
+// flattened stage A applies (so of every pair that can set a bit), and those pairs go to stage B.
+constexpr int kGbBuckets = 64;
+constexpr int kGbLevels = 6;     // spans 1 .. 32 buckets; 64 or more is the full mask
+constexpr int kGbMaxWords = 8;   // N <= 256
+constexpr int kGbList = 256;     // (grain slot, k) pairs per warp list
+
+__host__ __device__ inline bool grainwise_uses_bits(int n) { return n <= 32 * kGbMaxWords; }
+
+// The samples whose frac(offset) lies in the cyclic interval [c - h, c + h] (c in [0, 1)), rounded out
+// to whole buckets, written to m (kAnd = false) or ANDed into it (kAnd = true).
+template <int MW, bool kAnd>
+__device__ __forceinline__ void gb_axis_mask(const unsigned *tab, int W, float c, float h, int n, unsigned (&m)[MW]) {
+    const int blo = __float2int_rd(FG_FMUL(FG_FSUB(c, h), 64.0f));
+    const int bhi = __float2int_rd(FG_FMUL(FG_FADD(c, h), 64.0f));
+    const int len = bhi - blo + 1;
+    if (h >= 0.5f || len >= kGbBuckets) {
+        if (!kAnd) {
+#pragma unroll
+            for (int w = 0; w < MW; w++) {
+                const int rem = n - 32 * w;
+                m[w] = rem >= 32 ? 0xFFFFFFFFu : (rem > 0 ? (1u << rem) - 1u : 0u);
+            }
+        }
+        return;
+    }
+    const int b0 = blo & (kGbBuckets - 1);
+    const int L = 31 - __clz(len);
+    const unsigned *e0 = tab + (L * kGbBuckets + b0) * W;
+    const unsigned *e1 = tab + (L * kGbBuckets + ((b0 + len - (1 << L)) & (kGbBuckets - 1))) * W;
+#pragma unroll
+    for (int w = 0; w < MW; w++) {
+        const unsigned v = w < W ? (e0[w] | e1[w]) : 0u;
+        m[w] = kAnd ? (m[w] & v) : v;
+    }
+}
+
+template <bool kSmall, int MW>
+__device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int tile_x, int tile_y,
+                                                    unsigned char *smem_raw) {
+    const int W = (a.n + 31) >> 5;
+    float2 *offk = reinterpret_cast<float2 *>(smem_raw);                         // [n] (offx, offy) by k
+    unsigned *tabx = reinterpret_cast<unsigned *>(offk + ((a.n + 1) & ~1));     // [levels][buckets][W]
+    unsigned *taby = tabx + kGbLevels * kGbBuckets * W;
+    float4 *queue = reinterpret_cast<float4 *>(taby + kGbLevels * kGbBuckets * W);  // [warps][32] grains
+    unsigned *lists = reinterpret_cast<unsigned *>(queue + kGwWarps * 32);      // [warps][kGbList]
+    unsigned short *bk = reinterpret_cast<unsigned short *>(lists + kGwWarps * kGbList);  // [n] buckets
+    unsigned int *mask = reinterpret_cast<unsigned int *>(bk + ((a.n + 7) & ~7));
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    const int ix0 = tile_x * a.tin_w, iy0 = tile_y * a.tin_h;
+    const int ix1 = min(ix0 + a.tin_w, a.in_w), iy1 = min(iy0 + a.tin_h, a.in_h);
+    GwTile T;
+    T.rx0 = min(a.out_w, (int)floorf((float)ix0 * a.zoom));
+    T.ry0 = min(a.out_h, (int)floorf((float)iy0 * a.zoom));
+    T.rw = min(a.rmax_w, min(a.out_w, (int)floorf((float)ix1 * a.zoom)) - T.rx0);
+    T.rh = min(a.rmax_h, min(a.out_h, (int)floorf((float)iy1 * a.zoom)) - T.ry0);
+    T.rw = max(T.rw, 0);
+    T.rh = max(T.rh, 0);
+    T.words = a.words;
+    T.out_w = a.out_w;
+    T.flast_x = (float)(a.out_w - 1);
+    T.flast_y = (float)(a.out_h - 1);
+    T.gmask = a.gmask;
+    const int region_words = T.rw * T.rh * a.words;
+
+    // offsets by sample index, and each sample's x / y bucket
+    for (int i = tid; i < a.n; i += kGwThreads) {
+        const float4 e = a.sorted_offs[i];  // (frac(offy), offx, offy, k)
+        const int k = __float_as_int(e.w);
+        offk[k] = make_float2(e.y, e.z);
+        float fx = FG_FSUB(e.y, floorf(e.y));
+        if (!(fx < 1.0f)) fx = 0.0f;  // a tiny negative offset rounds up to 1; cyclically that is 0
+        bk[k] =(unsigned short)((int)FG_FMUL(fx, 64.0f) | ((int)FG_FMUL(e.x, 64.0f) << 8));
+    }
+    for (int t = tid; t < region_words; t += kGwThreads) mask[t] = 0u;
+    __syncthreads();
+    for (int t = tid; t < 2 * kGbBuckets * W; t += kGwThreads) {  // level 0: one bucket each
+        const int axis = t / (kGbBuckets * W), r = t - axis * kGbBuckets * W;
+        const int b = r / W, w = r - b * W;
+        unsigned bits = 0u;
+        for (int j = 0; j < 32; j++) {
+            const int k = w * 32 + j;
+            if (k < a.n && ((bk[k] >> (8 * axis)) & 0xFF) == b) bits |= 1u << j;
+        }
+        (axis ? taby : tabx)[b * W + w] = bits;
+    }
+    __syncthreads();
+    for (int L = 1; L < kGbLevels; L++) {
+        for (int t = tid; t < 2 * kGbBuckets * W; t += kGwThreads) {
+            const int axis = t / (kGbBuckets * W), r = t - axis * kGbBuckets * W;
+            const int b = r / W, w = r - b * W;
+            unsigned *tb = axis ? taby : tabx;
+            const int b2 = (b + (1 << (L - 1))) & (kGbBuckets - 1);
+            tb[(L * kGbBuckets + b) * W + w] = tb[((L - 1) * kGbBuckets + b) * W + w] |
+                                               tb[((L - 1) * kGbBuckets + b2) * W + w];
+        }
+        __syncthreads();
+    }
+
+    const int fw = ix1 - ix0, total = fw * (iy1 - iy0);
+    const UniformF32 U = uniform_f32_new(0.0f, 1.0f);
+    const float zoom = a.zoom;
+    float4 *q = queue + warp * 32;
+    unsigned *list = lists + warp * kGbList;
+
+    for (int base = warp * 32; base < total; base += kGwThreads) {
+        // one footprint pixel per lane, Poisson set-up in step across the warp
+        const int pi = base + lane;
+        uint32_t left = 0;
+        int px = 0, py = 0;
+        Xoshiro rng = {0, 0, 0, 0};
+        if (pi < total) {
+            px = ix0 + pi % fw;
+            py = iy0 + pi / fw;
+            const float lv = a.lam[(long long)py * a.in_w + px];
+            if (lv > 0.0f) {
+                rng = pixel_rng(a.seed, px, py);
+                const PoissonParams P = poisson_new((double)lv);
+                left = poisson_sample(P, rng);
+            }
+        }
+        while (__any_sync(0xffffffffu, left > 0)) {
+            // one grain per lane; its candidate samples as a bitmask
+            unsigned m[MW];
+#pragma unroll
+            for (int w = 0; w < MW; w++) m[w] = 0u;
+            int cnt = 0;
+            if (left > 0) {
+                left--;
+                const float cx = FG_FADD((float)px, uniform_f32_from(U, rng.next()));
+                const float cy = FG_FADD((float)py, uniform_f32_from(U, rng.next()));
+                float r = a.lognorm ? lognormal_radius_f32(a.log_mu, a.log_sigma, rng) : a.radius_mean;
+                if (r > a.rm) r = a.rm;
+                if (r > 0.0f) {
+                    const float ro = FG_FMUL(r, zoom);
+                    if (ro > 0.0f) {
+                        const float czx = FG_FMUL(cx, zoom), czy = FG_FMUL(cy, zoom);
+                        float cyf = FG_FSUB(0.5f, FG_FSUB(czy, floorf(czy)));  // frac(1/2 - czy)
+                        if (cyf < 0.0f) cyf = FG_FADD(cyf, 1.0f);
+                        float cxf = FG_FSUB(0.5f, FG_FSUB(czx, floorf(czx)));  // frac(1/2 - czx)
+                        if (cxf < 0.0f) cxf = FG_FADD(cxf, 1.0f);
+                        q[lane] = make_float4(czx, czy, ro, cyf);
+                        const float h = FG_FADD(ro, a.frac_eps);
+                        gb_axis_mask<MW, false>(tabx, W, cxf, h, a.n, m);
+                        gb_axis_mask<MW, true>(taby, W, cyf, h, a.n, m);
+#pragma unroll
+                        for (int w = 0; w < MW; w++) cnt += __popc(m[w]);
+                    }
+                }
+            }
+            // this step's (grain, sample) pairs, in lane order, through the list in chunks
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int tot = __shfl_sync(0xffffffffu, incl, 31);
+            const int excl = incl - cnt;
+            __syncwarp();
+            for (int done = 0; done < tot; done += kGbList) {
+                const int lim = done + kGbList;
+                if (cnt > 0 && excl < lim && excl + cnt > done) {
+                    int j = excl;
+#pragma unroll
+                    for (int w = 0; w < MW; w++) {
+                        unsigned mm = m[w];
+                        while (mm != 0u && j < lim) {
+                            const int bit = __ffs(mm) - 1;
+                            mm &= mm - 1u;
+                            if (j >= done) list[j - done] = ((unsigned)lane << 16) | (unsigned)(w * 32 + bit);
+                            j++;
+                        }
+                    }
+                }
+                __syncwarp();
+                const int nl = min(kGbList, tot - done);
+                for (int b = 0; b < nl; b += 32) {
+                    if (b + lane < nl) {
+                        const unsigned v = list[b + lane];
+                        const int k = (int)(v & 0xFFFFu);
+                        const float2 o = offk[k];
+                        gw_splat<kSmall>(T, mask, q[v >> 16], make_float4(0.0f, o.x, o.y, __int_as_float(k)));
+                    }
+                }
+                __syncwarp();
+            }
+        }
+    }
+    __syncthreads();
+
+    // OR the rectangle's words into the global mask (other CTAs' spills land there too).
+    for (int t = tid; t < region_words; t += kGwThreads) {
+        const unsigned v = mask[t];
+        if (v) {
+            const int w = t % a.words, px = t / a.words;
+            const int lx = px % T.rw, ly = px / T.rw;
+            atomicOr(a.gmask + ((long long)(T.ry0 + ly) * a.out_w + (T.rx0 + lx)) * a.words + w, v);
+        }
+    }
+}
+
+inline size_t grainwise_bits_smem_bytes(const GrainwiseArgs &a) {
+    const size_t W = (size_t)(a.n + 31) / 32;
+    return (size_t)((a.n + 1) & ~1) * sizeof(float2) + 2 * (size_t)kGbLevels * kGbBuckets * W * sizeof(unsigned) +
+           (size_t)kGwWarps * 32 * sizeof(float4) + (size_t)kGwWarps * kGbList * sizeof(unsigned) +
+           (size_t)((a.n + 7) & ~7) * sizeof(unsigned short) +
+           (size_t)a.rmax_w * a.rmax_h * a.words * sizeof(unsigned int);
+}
+
+// The tile variant for n samples: 4 or 8 = the bitmask filter with that many mask words, 0 = the
+// flattened stage A (n > 256).
+__host__ __device__ inline int grainwise_variant(int n) { return n <= 128 ? 4 : (grainwise_uses_bits(n) ? 8 : 0); }
+
 template <bool kSmall>
+__device__ __forceinline__ void grainwise_tile_flat(const GrainwiseArgs &a, int tile_x, int tile_y,
+                                                    unsigned char *smem_raw);
+
+// One input tile of the grain-wise kernel (all threads of the CTA; `smem_raw` holds its shared memory).
+// kVariant: grainwise_variant(a.n), or -1 to dispatch at run time (the batched kernel).
+template <bool kSmall, int kVariant = -1>
 __device__ __forceinline__ void grainwise_tile(const GrainwiseArgs &a, int tile_x, int tile_y,
                                                unsigned char *smem_raw) {
+    const int v = kVariant >= 0 ? kVariant : grainwise_variant(a.n);
+    if (v == 4) grainwise_tile_bits<kSmall, 4>(a, tile_x, tile_y, smem_raw);
+    else if (v == 8) grainwise_tile_bits<kSmall, kGbMaxWords>(a, tile_x, tile_y, smem_raw);
+    else grainwise_tile_flat<kSmall>(a, tile_x, tile_y, smem_raw);
+}
+
+template <bool kSmall>
+__device__ __forceinline__ void grainwise_tile_flat(const GrainwiseArgs &a, int tile_x, int tile_y,
+                                                    unsigned char *smem_raw) {
     float4 *tab = reinterpret_cast<float4 *>(smem_raw);                   // [n] offsets, by frac(offx)
     float4 *queue = tab + a.n;                                            // [warps][kGwQueue] grains
     uint2 *qrange = reinterpret_cast<uint2 *>(queue + kGwWarps * kGwQueue); // [warps][kGwQueue]
@@ -298,6 +532,7 @@ __device__ __forceinline__ void grainwise_tile(const GrainwiseArgs &a, int tile_
 
 // Shared-memory bytes of one grain-wise tile.
 inline size_t grainwise_tile_smem_bytes(const GrainwiseArgs &a) {
+    if (grainwise_uses_bits(a.n)) return grainwise_bits_smem_bytes(a);
     return (size_t)a.n * sizeof(float4) + (size_t)kGwWarps * kGwQueue * sizeof(float4) +
            (size_t)kGwWarps * kGwQueue * sizeof(uint2) + (size_t)kGwWarps * kGwList * sizeof(unsigned) +
            (size_t)a.n * sizeof(float) + ((size_t)kGwWarps * 33 + kGwBuckets + 3) * sizeof(int) +
