@@ -211,11 +211,28 @@ size_t grainwise_mask_bytes(const fg_params &p, const fg_derived &d) {
     return (size_t)d.output_width * d.output_height * ((p.n_samples + 31) / 32) * sizeof(unsigned int);
 }
 
+// Stream-ordered device buffer that frees itself.
+struct DevBuf {
+    void *p = nullptr;
+    cudaStream_t s = nullptr;
+    cudaError_t alloc(size_t bytes, cudaStream_t st) {
+        s = st;
+        return cudaMallocAsync(&p, bytes ? bytes : 16, st);
+    }
+    ~DevBuf() {
+        if (p) cudaFreeAsync(p, s);
+    }
+};
+
 fg_status enqueue_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
     if (grainwise_smem_bytes(a) > 200 * 1024)
         return set_error(FG_ERR_UNSUPPORTED, "n_samples too large for the grain-wise tile");
     FG_CUDA(cudaMemsetAsync(a.gmask, 0, (size_t)a.out_w * a.out_h * a.words * sizeof(unsigned int), s), "memset mask");
-    FG_CUDA(launch_grainwise(a, s), "grainwise kernel");
+    GrainwiseArgs b = a;
+    DevBuf work;  // the tile scheduler's area, freed in stream order after the launch
+    FG_CUDA(work.alloc(grainwise_work_ints(a) * sizeof(int), s), "alloc tile scheduler");
+    b.work = static_cast<int *>(work.p);
+    FG_CUDA(launch_grainwise(b, s), "grainwise kernel");
     return FG_OK;
 }
 
@@ -235,19 +252,6 @@ fg_status enqueue_grainwise_epilogue(const GrainwiseArgs &a, float *d_out, int m
     FG_CUDA(launch_grainwise_epilogue(e, s), "grainwise epilogue");
     return FG_OK;
 }
-
-// Stream-ordered device buffer that frees itself.
-struct DevBuf {
-    void *p = nullptr;
-    cudaStream_t s = nullptr;
-    cudaError_t alloc(size_t bytes, cudaStream_t st) {
-        s = st;
-        return cudaMallocAsync(&p, bytes ? bytes : 16, st);
-    }
-    ~DevBuf() {
-        if (p) cudaFreeAsync(p, s);
-    }
-};
 
 static void keep_pool_memory() {
     static bool done = false;

@@ -30,12 +30,90 @@
 #include "fg_grainwise.cuh"
 #include "fg_internal.h"
 
+#include <algorithm>
+
 namespace fg {
 
 template <bool kSmall, int kVariant>
 __global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const __grid_constant__ GrainwiseArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     grainwise_tile<kSmall, kVariant>(a, blockIdx.x, blockIdx.y, smem_raw);
+}
+
+// Persistent form: CTAs pull tiles from the scheduler's list (a.work[2..], heaviest first) through the
+// counter a.work[0] until the list is exhausted.
+template <bool kSmall, int kVariant>
+__global__ void __launch_bounds__(kGwThreads, 2) grainwise_persistent_kernel(const __grid_constant__ GrainwiseArgs a,
+                                                                             int ntx, int ntiles) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_tile;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int i = atomicAdd(a.work, 1);
+            s_tile = i < ntiles ? a.work[2 + i] : -1;
+        }
+        __syncthreads();
+        const int t = s_tile;
+        if (t < 0) break;
+        grainwise_tile<kSmall, kVariant>(a, t % ntx, t / ntx, smem_raw);
+        __syncthreads();
+    }
+}
+
+// Expected cost of each input tile (one warp per tile): its grains (sum of lambda) plus a per-pixel
+// set-up term.
+__global__ void grainwise_costs_kernel(const float *__restrict__ lam, int in_w, int in_h, int tin_w, int tin_h, int ntx,
+                                       int ntiles, float *__restrict__ cost) {
+    const int tile = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (tile >= ntiles) return;
+    const int x0 = (tile % ntx) * tin_w, y0 = (tile / ntx) * tin_h;
+    const int w = min(x0 + tin_w, in_w) - x0, n = w * (min(y0 + tin_h, in_h) - y0);
+    float sum = 0.0f;
+    for (int i = lane; i < n; i += 32) sum += lam[(long long)(y0 + i / w) * in_w + x0 + i % w];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) cost[tile] = sum + 4.0f * (float)n;
+}
+
+// order[i] = the tile indices by descending cost: a bitonic sort in shared memory (one CTA) for up to
+// kGwSortMax tiles; larger grids keep the natural order.
+constexpr int kGwSortMax = 4096;
+__global__ void __launch_bounds__(1024) grainwise_order_kernel(const float *__restrict__ cost, int ntiles,
+                                                               int *__restrict__ order) {
+    __shared__ float key[kGwSortMax];
+    __shared__ int idx[kGwSortMax];
+    const int tid = threadIdx.x;
+    if (ntiles > kGwSortMax) {
+        for (int i = tid; i < ntiles; i += blockDim.x) order[i] = i;
+        return;
+    }
+    int n2 = 2;
+    while (n2 < ntiles) n2 <<= 1;
+    for (int i = tid; i < n2; i += blockDim.x) {
+        key[i] = i < ntiles ? cost[i] : -1.0f;  // costs are >= 0: the padding sorts last
+        idx[i] = i;
+    }
+    __syncthreads();
+    for (int k = 2; k <= n2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < n2; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const bool desc = (i & k) == 0;
+                    if ((key[i] < key[ixj]) == desc) {
+                        const float tk = key[i];
+                        key[i] = key[ixj];
+                        key[ixj] = tk;
+                        const int ti = idx[i];
+                        idx[i] = idx[ixj];
+                        idx[ixj] = ti;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = tid; i < ntiles; i += blockDim.x) order[i] = idx[i];
 }
 
 // popcount * (1/N) of the sample masks (src/grainwise.rs:114-122), fused with the colour output:
@@ -86,18 +164,51 @@ bool grainwise_small_coords(const GrainwiseArgs &a) {
     return span < 4194304.0f;
 }
 
+int grainwise_tile_count(const GrainwiseArgs &a) {
+    return ((a.in_w + a.tin_w - 1) / a.tin_w) * ((a.in_h + a.tin_h - 1) / a.tin_h);
+}
+
+size_t grainwise_work_ints(const GrainwiseArgs &a) { return 2 + 2 * (size_t)grainwise_tile_count(a); }
+
 cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
     const size_t smem = grainwise_smem_bytes(a);
-    dim3 grid((a.in_w + a.tin_w - 1) / a.tin_w, (a.in_h + a.tin_h - 1) / a.tin_h);
-    if (grid.x == 0 || grid.y == 0) return cudaSuccess;
+    const int ntx = (a.in_w + a.tin_w - 1) / a.tin_w, nty = (a.in_h + a.tin_h - 1) / a.tin_h;
+    if (ntx <= 0 || nty <= 0) return cudaSuccess;
     const bool small = grainwise_small_coords(a);
     const int v = grainwise_variant(a.n);
-    void (*k)(GrainwiseArgs);
-    if (small) k = v == 4 ? grainwise_kernel<true, 4> : (v == 8 ? grainwise_kernel<true, 8> : grainwise_kernel<true, 0>);
-    else k = v == 4 ? grainwise_kernel<false, 4> : (v == 8 ? grainwise_kernel<false, 8> : grainwise_kernel<false, 0>);
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e;
+    if (!a.work) {
+        void (*k)(GrainwiseArgs);
+        if (small) k = v == 4 ? grainwise_kernel<true, 4> : (v == 8 ? grainwise_kernel<true, 8> : grainwise_kernel<true, 0>);
+        else k = v == 4 ? grainwise_kernel<false, 4> : (v == 8 ? grainwise_kernel<false, 8> : grainwise_kernel<false, 0>);
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<dim3(ntx, nty), kGwThreads, smem, s>>>(a);
+        return cudaGetLastError();
+    }
+    // tile scheduler: costs from lambda, heaviest first, persistent CTAs
+    const int ntiles = ntx * nty;
+    float *cost = reinterpret_cast<float *>(a.work + 2 + ntiles);
+    e = cudaMemsetAsync(a.work, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
-    k<<<grid, kGwThreads, smem, s>>>(a);
+    grainwise_costs_kernel<<<(ntiles + 7) / 8, 256, 0, s>>>(a.lam, a.in_w, a.in_h, a.tin_w, a.tin_h, ntx, ntiles, cost);
+    grainwise_order_kernel<<<1, 1024, 0, s>>>(cost, ntiles, a.work + 2);
+    void (*k)(GrainwiseArgs, int, int);
+    if (small)
+        k = v == 4 ? grainwise_persistent_kernel<true, 4>
+                   : (v == 8 ? grainwise_persistent_kernel<true, 8> : grainwise_persistent_kernel<true, 0>);
+    else
+        k = v == 4 ? grainwise_persistent_kernel<false, 4>
+                   : (v == 8 ? grainwise_persistent_kernel<false, 8> : grainwise_persistent_kernel<false, 0>);
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kGwThreads, smem);
+    if (e != cudaSuccess) return e;
+    const int grid = std::max(1, std::min(ntiles, sms * std::max(1, per_sm)));
+    k<<<grid, kGwThreads, smem, s>>>(a, ntx, ntiles);
     return cudaGetLastError();
 }
 

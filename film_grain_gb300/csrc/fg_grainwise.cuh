@@ -183,7 +183,6 @@ __device__ __forceinline__ void gw_raster_batch(const GwTile &T, unsigned int *m
 constexpr int kGbBuckets = 64;
 constexpr int kGbLevels = 6;     // spans 1 .. 32 buckets; 64 or more is the full mask
 constexpr int kGbMaxWords = 8;   // N <= 256
-constexpr int kGbList = 256;     // (grain slot, k) pairs per warp list
 
 __host__ __device__ inline bool grainwise_uses_bits(int n) { return n <= 32 * kGbMaxWords; }
 
@@ -222,11 +221,10 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
     float2 *offk = reinterpret_cast<float2 *>(smem_raw);                         // [n] (offx, offy) by k
     unsigned *tabx = reinterpret_cast<unsigned *>(offk + ((a.n + 1) & ~1));     // [levels][buckets][W]
     unsigned *taby = tabx + kGbLevels * kGbBuckets * W;
-    float4 *queue = reinterpret_cast<float4 *>(taby + kGbLevels * kGbBuckets * W);  // [warps][32] grains
-    unsigned *lists = reinterpret_cast<unsigned *>(queue + kGwWarps * 32);      // [warps][kGbList]
-    unsigned short *bk = reinterpret_cast<unsigned short *>(lists + kGwWarps * kGbList);  // [n] buckets
-    unsigned int *mask = reinterpret_cast<unsigned int *>(bk + ((a.n + 7) & ~7));
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    unsigned short *bk = reinterpret_cast<unsigned short *>(taby + kGbLevels * kGbBuckets * W);  // [n] buckets
+    int *next_px = reinterpret_cast<int *>(bk + ((a.n + 7) & ~7));             // [4]: batch counter
+    unsigned int *mask = reinterpret_cast<unsigned int *>(next_px + 4);
+    const int tid = threadIdx.x, lane = tid & 31;
 
     const int ix0 = tile_x * a.tin_w, iy0 = tile_y * a.tin_h;
     const int ix1 = min(ix0 + a.tin_w, a.in_w), iy1 = min(iy0 + a.tin_h, a.in_h);
@@ -254,6 +252,7 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
         bk[k] =(unsigned short)((int)FG_FMUL(fx, 64.0f) | ((int)FG_FMUL(e.x, 64.0f) << 8));
     }
     for (int t = tid; t < region_words; t += kGwThreads) mask[t] = 0u;
+    if (tid == 0) *next_px = 0;
     __syncthreads();
     for (int t = tid; t < 2 * kGbBuckets * W; t += kGwThreads) {  // level 0: one bucket each
         const int axis = t / (kGbBuckets * W), r = t - axis * kGbBuckets * W;
@@ -281,11 +280,13 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
     const int fw = ix1 - ix0, total = fw * (iy1 - iy0);
     const UniformF32 U = uniform_f32_new(0.0f, 1.0f);
     const float zoom = a.zoom;
-    float4 *q = queue + warp * 32;
-    unsigned *list = lists + warp * kGbList;
-
-    for (int base = warp * 32; base < total; base += kGwThreads) {
-        // one footprint pixel per lane, Poisson set-up in step across the warp
+    for (;;) {
+        // the next 32 footprint pixels of the tile (a shared counter balances the warps), one per
+        // lane, Poisson set-up in step across the warp
+        int base = 0;
+        if (lane == 0) base = atomicAdd(next_px, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) break;
         const int pi = base + lane;
         uint32_t left = 0;
         int px = 0, py = 0;
@@ -306,6 +307,7 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
 #pragma unroll
             for (int w = 0; w < MW; w++) m[w] = 0u;
             int cnt = 0;
+            float gx = 0.0f, gy = 0.0f, gr = 0.0f;  // this lane's grain: zoomed centre, zoomed radius
             if (left > 0) {
                 left--;
                 const float cx = FG_FADD((float)px, uniform_f32_from(U, rng.next()));
@@ -320,7 +322,9 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
                         if (cyf < 0.0f) cyf = FG_FADD(cyf, 1.0f);
                         float cxf = FG_FSUB(0.5f, FG_FSUB(czx, floorf(czx)));  // frac(1/2 - czx)
                         if (cxf < 0.0f) cxf = FG_FADD(cxf, 1.0f);
-                        q[lane] = make_float4(czx, czy, ro, cyf);
+                        gx = czx;
+                        gy = czy;
+                        gr = ro;
                         const float h = FG_FADD(ro, a.frac_eps);
                         gb_axis_mask<MW, false>(tabx, W, cxf, h, a.n, m);
                         gb_axis_mask<MW, true>(taby, W, cyf, h, a.n, m);
@@ -329,7 +333,10 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
                     }
                 }
             }
-            // this step's (grain, sample) pairs, in lane order, through the list in chunks
+            // this step's (grain, sample) pairs, 32 at a time: pair p belongs to the first lane whose
+            // inclusive candidate count exceeds p (a binary search over shuffled prefixes), and is the
+            // (p - exclusive count)-th set bit of that lane's mask.  Every lane stays converged and the
+            // grains never leave the registers of the lanes that drew them.
             int incl = cnt;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -337,34 +344,44 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
                 if (lane >= o) incl += y;
             }
             const int tot = __shfl_sync(0xffffffffu, incl, 31);
-            const int excl = incl - cnt;
-            __syncwarp();
-            for (int done = 0; done < tot; done += kGbList) {
-                const int lim = done + kGbList;
-                if (cnt > 0 && excl < lim && excl + cnt > done) {
-                    int j = excl;
+            for (int b = 0; b < tot; b += 32) {
+                const int p = b + lane;
+                int src = 0;
 #pragma unroll
-                    for (int w = 0; w < MW; w++) {
-                        unsigned mm = m[w];
-                        while (mm != 0u && j < lim) {
-                            const int bit = __ffs(mm) - 1;
-                            mm &= mm - 1u;
-                            if (j >= done) list[j - done] = ((unsigned)lane << 16) | (unsigned)(w * 32 + bit);
-                            j++;
-                        }
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int v = __shfl_sync(0xffffffffu, incl, src + step - 1);
+                    if (v <= p) src += step;
+                }
+                int j = p - (__shfl_sync(0xffffffffu, incl, src) - __shfl_sync(0xffffffffu, cnt, src));
+                unsigned word = 0u;
+                int wsel = 0;
+#pragma unroll
+                for (int w = 0; w < MW; w++) {
+                    const unsigned mw = __shfl_sync(0xffffffffu, m[w], src);
+                    const int c = __popc(mw);
+                    if (wsel == w) {
+                        if (j < c) word = mw;
+                        else { j -= c; wsel = w + 1; }
                     }
                 }
-                __syncwarp();
-                const int nl = min(kGbList, tot - done);
-                for (int b = 0; b < nl; b += 32) {
-                    if (b + lane < nl) {
-                        const unsigned v = list[b + lane];
-                        const int k = (int)(v & 0xFFFFu);
-                        const float2 o = offk[k];
-                        gw_splat<kSmall>(T, mask, q[v >> 16], make_float4(0.0f, o.x, o.y, __int_as_float(k)));
+                int bit = 0;  // the j-th set bit of `word`
+#pragma unroll
+                for (int half = 16; half > 0; half >>= 1) {
+                    const int c = __popc(word & ((1u << half) - 1u));
+                    if (j >= c) {
+                        j -= c;
+                        bit += half;
+                        word >>= half;
                     }
                 }
-                __syncwarp();
+                const float sx = __shfl_sync(0xffffffffu, gx, src);
+                const float sy = __shfl_sync(0xffffffffu, gy, src);
+                const float sr = __shfl_sync(0xffffffffu, gr, src);
+                if (p < tot) {
+                    const int k = wsel * 32 + bit;
+                    const float2 o = offk[k];
+                    gw_splat<kSmall>(T, mask, make_float4(sx, sy, sr, 0.0f), make_float4(0.0f, o.x, o.y, __int_as_float(k)));
+                }
             }
         }
     }
@@ -384,8 +401,7 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
 inline size_t grainwise_bits_smem_bytes(const GrainwiseArgs &a) {
     const size_t W = (size_t)(a.n + 31) / 32;
     return (size_t)((a.n + 1) & ~1) * sizeof(float2) + 2 * (size_t)kGbLevels * kGbBuckets * W * sizeof(unsigned) +
-           (size_t)kGwWarps * 32 * sizeof(float4) + (size_t)kGwWarps * kGbList * sizeof(unsigned) +
-           (size_t)((a.n + 7) & ~7) * sizeof(unsigned short) +
+           (size_t)((a.n + 7) & ~7) * sizeof(unsigned short) + 4 * sizeof(int) +
            (size_t)a.rmax_w * a.rmax_h * a.words * sizeof(unsigned int);
 }
 

@@ -61,6 +61,7 @@ struct GrainwiseArgs {
     int lognorm;
     float radius_mean;
     double log_mu, log_sigma;
+    int *work;                  // null: one CTA per tile; else the tile scheduler's area (grainwise_work_ints)
 };
 
 // popcount / colour epilogue of the grain-wise path.
@@ -90,6 +91,8 @@ cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, size_t smem, cudaS
 size_t pixelwise_smem_bytes();
 cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s);
 size_t grainwise_smem_bytes(const GrainwiseArgs &a);
+int grainwise_tile_count(const GrainwiseArgs &a);
+size_t grainwise_work_ints(const GrainwiseArgs &a);  // scheduler area: counter, pad, order[tiles], cost[tiles]
 cudaError_t launch_grainwise_epilogue(const GrainwiseEpilogueArgs &a, cudaStream_t s);
 cudaError_t launch_epilogue(const EpilogueArgs &a, cudaStream_t s);
 cudaError_t launch_rgb_pack(const float *p0, const float *p1, const float *p2, int n, unsigned char *out,
