@@ -554,7 +554,8 @@ def main():
     sp = stream.cuda_stream
     offs = np.ascontiguousarray(derived.offsets if wl["algo"] == "grain" else derived.offsets_input, np.float32)
     fn = L.fg_render_grainwise_async if wl["algo"] == "grain" else L.fg_render_pixelwise_async
-    launches_per_plane = 2 if wl["algo"] == "grain" else 3  # grain: raster, popcount; pixel: cells, tiles, epilogue
+    # grain: tile costs, tile order, persistent tiles, popcount; pixel: cells, tiles, epilogue
+    launches_per_plane = 4 if wl["algo"] == "grain" else 3
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     ev = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in planes] for _ in range(args.steps)]
@@ -670,7 +671,7 @@ def main():
                             "frac": ach / peak, "traffic": GRAINWISE_DRAM_BYTES_PER_OUT_PX * ow * oh,
                             "traffic_basis": "ncu dram bytes of the grain_rgb_512 launch "
                                              "(profiles/grainwise_kernel_grain_rgb_512_ncu.md), scaled by output pixels",
-                            "kernel": "grainwise_kernel", "launch_ms": launch_ms,
+                            "kernel": "grainwise_persistent_kernel (launch_ms: the whole plane)", "launch_ms": launch_ms,
                             "lane_ops_per_launch": ops, "counts": counts,
                             "peak_basis": f"{sm_count} SMs x 128 lanes x {f_mhz:.0f} MHz (sampled)"}
     print(json.dumps(line), flush=True)
