@@ -239,41 +239,65 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
 
         bool staged = false;
         if (window_fits) {
-            // ---- pass A: grain count per window cell.  Each thread walks a contiguous run of cells in
-            // column-major order, so the column stage of the cell hash and the lambda pixel's Poisson
-            // set-up are reused along the run; counts are stored row-major (the CSR order).
+            // ---- pass A1: which window cells hold grains.  The first uniform alone decides q == 0
+            // (cell_count_h), so every cell costs the same; each thread walks a contiguous run of cells
+            // in column-major order, reusing the column stage of the cell hash and the lambda pixel's
+            // Poisson set-up along the run.  Empty cells get count 0; the others join the list
+            // (one shared atomic per warp step) and get their count in A2.
             {
                 const int per = (nc + kPwThreads - 1) / kPwThreads;
                 const int c0 = tid * per, c1 = min(nc, c0 + per);
+                const int lane = tid & 31;
                 int ci = c0 / (int)Hc, cj = c0 % (int)Hc;
                 int col = -1, pix = -1;
                 uint64_t colh = 0;
                 long long thresh = 0;
-                double exp_lambda = 0.0;
-                for (int c = c0; c < c1; c++) {
-                    if (ci != col) {
-                        col = ci;
-                        colh = cell_col_hash(a.seed, wi0 + ci);
+                for (int step = 0; step < per; step++) {
+                    const int c = c0 + step;
+                    bool nonempty = false;
+                    int rc = 0;
+                    if (c < c1) {
+                        if (ci != col) {
+                            col = ci;
+                            colh = cell_col_hash(a.seed, wi0 + ci);
+                        }
+                        const int p = S.rowiy[cj] * a.in_w + S.colix[ci];
+                        if (p != pix) {
+                            pix = p;
+                            thresh = a.cells[p].thresh;
+                        }
+                        const uint64_t h = cell_row_hash(colh, wj0 + cj);
+                        const uint64_t s0 = fmix64(h + kPhi), s3 = fmix64(h + 4 * kPhi);
+                        const long long v = (long long)((rotl64(s0 + s3, 23) + s0) >> 11);
+                        rc = cj * (int)Wc + ci;
+                        nonempty = v > thresh;
+                        if (!nonempty) S.pre[rc] = 0;
+                        if (++cj == (int)Hc) {
+                            cj = 0;
+                            ci++;
+                        }
                     }
-                    const int p = S.rowiy[cj] * a.in_w + S.colix[ci];
-                    if (p != pix) {
-                        pix = p;
-                        const CellParam cp = a.cells[p];
-                        thresh = cp.thresh;
-                        exp_lambda = cp.exp_lambda;
+                    const unsigned nb = __ballot_sync(0xffffffffu, nonempty);
+                    if (nb) {
+                        int slot0 = 0;
+                        if (lane == __ffs(nb) - 1) slot0 = atomicAdd(&S.nlist, __popc(nb));
+                        slot0 = __shfl_sync(0xffffffffu, slot0, __ffs(nb) - 1);
+                        if (nonempty) S.list[slot0 + __popc(nb & ((1u << lane) - 1u))] = (unsigned short)rc;
                     }
+                }
+            }
+            __syncthreads();
+            // ---- pass A2: the grain counts of the non-empty cells, one cell per thread
+            {
+                const int nl = S.nlist;
+                for (int t = tid; t < nl; t += kPwThreads) {
+                    const int rc = S.list[t];
+                    const int ci = rc % (int)Wc, cj = rc / (int)Wc;
+                    const CellParam cp = a.cells[(long long)S.rowiy[cj] * a.in_w + S.colix[ci]];
                     Xoshiro rng;
-                    const uint32_t q = cell_count_h(cell_row_hash(colh, wj0 + cj), thresh, exp_lambda, rng);
-                    const int rc = cj * (int)Wc + ci;
+                    const uint32_t q = cell_count_h(cell_row_hash(cell_col_hash(a.seed, wi0 + ci), wj0 + cj), cp.thresh,
+                                                    cp.exp_lambda, rng);
                     S.pre[rc] = (unsigned short)(q > 65535u ? 65535u : q);
-                    if (q) {
-                        const int slot = atomicAdd(&S.nlist, 1);
-                        S.list[slot] = (unsigned short)rc;
-                    }
-                    if (++cj == (int)Hc) {
-                        cj = 0;
-                        ci++;
-                    }
                 }
             }
             __syncthreads();
