@@ -62,108 +62,180 @@ struct SgConvArgs {
     int H, W, in_cstride, tiles_x, tiles_per_img;
 };
 
-// 3x3 conv of CIN channels to COUT channels.  The element strides in shared memory (CIN + 8 per pixel,
-// 9*CIN + 8 per weight row) make the fragment loads of the 8 row groups hit disjoint bank quadruples.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, bool valid) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 16 : 0));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const bf16 *smem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(sa));
+}
+__device__ __forceinline__ void ldsm_x2(uint32_t (&r)[2], const bf16 *smem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r[0]), "=r"(r[1]) : "r"(sa));
+}
+
+// Shared-memory bytes of the conv kernel: the weights plus two input-tile stages.
+template <int CIN, int COUT>
+constexpr int sg_conv_smem_bytes() {
+    return (COUT * (9 * CIN + 8) + 2 * kSgHH * kSgHW * (CIN + 8)) * 2;
+}
+
+// 3x3 conv of CIN channels to COUT channels over all tiles of the batch.  Persistent: a CTA loads the
+// weights once, then walks tiles with a grid stride, fetching the next tile's haloed input into the
+// other shared-memory stage with cp.async (zero-filled outside the image) while the tensor cores work
+// on the current one.  Fragments come from ldmatrix; the element strides (CIN + 8 per pixel, 9*CIN + 8
+// per weight row) put the 8 rows of every ldmatrix phase in disjoint banks.
 template <int CIN, int COUT, int MODE>
-__global__ void __launch_bounds__(kSgThreads) sg_conv_fwd(const __grid_constant__ SgConvArgs a) {
+__global__ void __launch_bounds__(kSgThreads) sg_conv_fwd(const __grid_constant__ SgConvArgs a, int total_tiles) {
     constexpr int PS = CIN + 8;
     constexpr int K = 9 * CIN;
     constexpr int WS = K + 8;
     constexpr int NT = COUT / 8;
-    __shared__ __align__(16) bf16 s_in[kSgHH * kSgHW * PS];
-    __shared__ __align__(16) bf16 s_w[COUT * WS];
+    constexpr int STAGE = kSgHH * kSgHW * PS;
+    extern __shared__ __align__(16) unsigned char sg_smem[];
+    bf16 *s_w = reinterpret_cast<bf16 *>(sg_smem);
+    bf16 *s_stage = s_w + COUT * WS;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int img = blockIdx.x / a.tiles_per_img;
-    const int t = blockIdx.x - img * a.tiles_per_img;
-    const int y0 = (t / a.tiles_x) * kSgTH, x0 = (t % a.tiles_x) * kSgTW;
     const int H = a.H, W = a.W;
-    const size_t img_off = (size_t)img * H * W;
 
-    // stage the haloed input tile (zeros outside the image) and the weights, 16 bytes per access
-    constexpr int C8 = CIN / 8;
-    for (int e = tid; e < kSgHH * kSgHW * C8; e += kSgThreads) {
-        const int c8 = e % C8, px = e / C8;
-        const int hx = px % kSgHW, hy = px / kSgHW;
-        const int gy = y0 + hy - 1, gx = x0 + hx - 1;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (gy >= 0 && gy < H && gx >= 0 && gx < W)
-            v = *reinterpret_cast<const uint4 *>(a.in + (img_off + (size_t)gy * W + gx) * a.in_cstride + 8 * c8);
-        *reinterpret_cast<uint4 *>(&s_in[px * PS + 8 * c8]) = v;
-    }
     constexpr int K8 = K / 8;
     for (int e = tid; e < COUT * K8; e += kSgThreads) {
         const int k8 = e % K8, n = e / K8;
-        *reinterpret_cast<uint4 *>(&s_w[n * WS + 8 * k8]) = *reinterpret_cast<const uint4 *>(a.w + (size_t)n * K + 8 * k8);
+        cp_async16(&s_w[n * WS + 8 * k8], a.w + (size_t)n * K + 8 * k8, true);
     }
-    __syncthreads();
+    auto load_tile = [&](int t, bf16 *dst) {
+        const int img = t / a.tiles_per_img, tt = t - img * a.tiles_per_img;
+        const int y0 = (tt / a.tiles_x) * kSgTH, x0 = (tt % a.tiles_x) * kSgTW;
+        const size_t img_off = (size_t)img * H * W;
+        constexpr int C8 = CIN / 8;
+        for (int e = tid; e < kSgHH * kSgHW * C8; e += kSgThreads) {
+            const int c8 = e % C8, px = e / C8;
+            const int hx = px % kSgHW, hy = px / kSgHW;
+            const int gy = y0 + hy - 1, gx = x0 + hx - 1;
+            const bool ok = gy >= 0 && gy < H && gx >= 0 && gx < W;
+            const bf16 *src = ok ? a.in + (img_off + (size_t)gy * W + gx) * a.in_cstride + 8 * c8 : a.in;
+            cp_async16(&dst[px * PS + 8 * c8], src, ok);
+        }
+    };
+    int t = blockIdx.x;
+    if (t < total_tiles) load_tile(t, s_stage);
+    cp_async_commit();  // the weights and the first tile
 
+    // ldmatrix lane addressing: A rows (pixels) 0-15 and k halves; B rows (output channels) and k halves
+    const int a_row = (lane & 7) + ((lane >> 3) & 1) * 8, a_k = (lane >> 4) * 8;
+    const int b_n = (lane & 7) + (lane >> 4) * 8, b_k = ((lane >> 3) & 1) * 8;
     const int g = lane >> 2, q = lane & 3;
-    float acc[2][NT][4];
+    // this lane's bias pairs, and whether the residual is the conv's own input (then it is read from the
+    // staged tile instead of global memory)
+    float bias0[NT], bias1[NT];
 #pragma unroll
-    for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-        for (int nt = 0; nt < NT; nt++)
-#pragma unroll
-            for (int r = 0; r < 4; r++) acc[mt][nt][r] = 0.0f;
+    for (int nt = 0; nt < NT; nt++) {
+        const bool used = MODE == kSgRelu || MODE == kSgResidual || (MODE == kSgOutput && nt == 0);
+        bias0[nt] = used ? a.bias[8 * nt + 2 * q] : 0.0f;
+        bias1[nt] = used && MODE != kSgOutput ? a.bias[8 * nt + 2 * q + 1] : 0.0f;
+    }
+    const bool res_staged = (MODE == kSgResidual || MODE == kSgLinearAdd) && a.res == a.in && a.in_cstride == COUT &&
+                            CIN == COUT;
+    int stage = 0;
+    for (; t < total_tiles; t += gridDim.x) {
+        if (t + (int)gridDim.x < total_tiles) load_tile(t + gridDim.x, s_stage + (stage ^ 1) * STAGE);
+        cp_async_commit();
+        cp_async_wait<1>();  // everything but the prefetch just issued has landed
+        __syncthreads();
+        const bf16 *s_in = s_stage + stage * STAGE;
 
+        float acc[2][NT][4];
 #pragma unroll
-    for (int tap = 0; tap < 9; tap++) {
-        const int ky = tap / 3, kx = tap % 3;
+        for (int mt = 0; mt < 2; mt++)
 #pragma unroll
-        for (int cb = 0; cb < CIN; cb += 16) {
-            const int kbase = tap * CIN + cb;
-            uint32_t bf[NT][2];
+            for (int nt = 0; nt < NT; nt++)
 #pragma unroll
-            for (int nt = 0; nt < NT; nt++) {
-                const bf16 *wr = &s_w[(nt * 8 + g) * WS + kbase + 2 * q];
-                bf[nt][0] = ld_u32(wr);
-                bf[nt][1] = ld_u32(wr + 8);
+                for (int r = 0; r < 4; r++) acc[mt][nt][r] = 0.0f;
+#pragma unroll
+        for (int tap = 0; tap < 9; tap++) {
+            const int ky = tap / 3, kx = tap % 3;
+#pragma unroll
+            for (int cb = 0; cb < CIN; cb += 16) {
+                const int kbase = tap * CIN + cb;
+                uint32_t bfr[NT][2];
+                if constexpr (NT >= 2) {
+#pragma unroll
+                    for (int np = 0; np < NT; np += 2) {
+                        uint32_t r[4];
+                        ldsm_x4(r, &s_w[(np * 8 + b_n) * WS + kbase + b_k]);
+                        bfr[np][0] = r[0];
+                        bfr[np][1] = r[1];
+                        bfr[np + 1][0] = r[2];
+                        bfr[np + 1][1] = r[3];
+                    }
+                } else {
+                    uint32_t r[2];
+                    ldsm_x2(r, &s_w[(lane & 7) * WS + kbase + b_k]);
+                    bfr[0][0] = r[0];
+                    bfr[0][1] = r[1];
+                }
+#pragma unroll
+                for (int mt = 0; mt < 2; mt++) {
+                    uint32_t af[4];
+                    ldsm_x4(af, &s_in[((warp + ky) * kSgHW + (16 * mt + a_row + kx)) * PS + cb + a_k]);
+#pragma unroll
+                    for (int nt = 0; nt < NT; nt++) mma_bf16(acc[mt][nt], af[0], af[1], af[2], af[3], bfr[nt][0], bfr[nt][1]);
+                }
             }
+        }
+
+        // epilogue: acc[mt][nt][r] is (pixel 16*mt + g + 8*(r>>1), channel 8*nt + 2*q + (r&1))
+        const int img = t / a.tiles_per_img, tt = t - img * a.tiles_per_img;
+        const int oy = (tt / a.tiles_x) * kSgTH + warp, x0 = (tt % a.tiles_x) * kSgTW;
+        const size_t img_off = (size_t)img * H * W;
+        if (oy < H) {
 #pragma unroll
             for (int mt = 0; mt < 2; mt++) {
-                // rows m = 16*mt + g (+8): pixels of tile row `warp`, shifted by the tap
-                const bf16 *r0 = &s_in[((warp + ky) * kSgHW + (16 * mt + g + kx)) * PS + cb + 2 * q];
-                const bf16 *r1 = r0 + 8 * PS;
-                const uint32_t a0 = ld_u32(r0), a1 = ld_u32(r1), a2 = ld_u32(r0 + 8), a3 = ld_u32(r1 + 8);
 #pragma unroll
-                for (int nt = 0; nt < NT; nt++) mma_bf16(acc[mt][nt], a0, a1, a2, a3, bf[nt][0], bf[nt][1]);
+                for (int half = 0; half < 2; half++) {
+                    const int ox = x0 + 16 * mt + g + 8 * half;
+                    if (ox >= W) continue;
+                    const size_t p = img_off + (size_t)oy * W + ox;
+                    if constexpr (MODE == kSgOutput) {
+                        if (q == 0) a.out_f32[p] = a.res_f32[p] + acc[mt][0][2 * half] + bias0[0];
+                    } else {
+                        // the output pixel's position in the staged (haloed) tile
+                        const bf16 *srow = &s_in[((warp + 1) * kSgHW + (16 * mt + g + 8 * half + 1)) * PS];
+#pragma unroll
+                        for (int nt = 0; nt < NT; nt++) {
+                            const int n = 8 * nt + 2 * q;
+                            float z0 = acc[mt][nt][2 * half], z1 = acc[mt][nt][2 * half + 1];
+                            if (MODE == kSgRelu || MODE == kSgResidual) {
+                                z0 = fmaxf(z0 + bias0[nt], 0.0f);
+                                z1 = fmaxf(z1 + bias1[nt], 0.0f);
+                            }
+                            if (MODE == kSgResidual && a.aux)
+                                *reinterpret_cast<__nv_bfloat162 *>(&a.aux[p * COUT + n]) = __floats2bfloat162_rn(z0, z1);
+                            if (MODE == kSgResidual || MODE == kSgLinearAdd) {
+                                const __nv_bfloat162 rv = res_staged
+                                                              ? *reinterpret_cast<const __nv_bfloat162 *>(&srow[n])
+                                                              : *reinterpret_cast<const __nv_bfloat162 *>(&a.res[p * COUT + n]);
+                                z0 += __bfloat162float(rv.x);
+                                z1 += __bfloat162float(rv.y);
+                            }
+                            *reinterpret_cast<__nv_bfloat162 *>(&a.out[p * COUT + n]) = __floats2bfloat162_rn(z0, z1);
+                        }
+                    }
+                }
             }
         }
+        __syncthreads();  // this stage is refilled by the next iteration's prefetch
+        stage ^= 1;
     }
-
-    // epilogue: acc[mt][nt][r] is (pixel 16*mt + g + 8*(r>>1), channel 8*nt + 2*q + (r&1))
-    const int oy = y0 + warp;
-    if (oy >= H) return;
-#pragma unroll
-    for (int mt = 0; mt < 2; mt++) {
-#pragma unroll
-        for (int half = 0; half < 2; half++) {
-            const int ox = x0 + 16 * mt + g + 8 * half;
-            if (ox >= W) continue;
-            const size_t p = img_off + (size_t)oy * W + ox;
-            if constexpr (MODE == kSgOutput) {
-                if (q == 0) a.out_f32[p] = a.res_f32[p] + acc[mt][0][2 * half] + a.bias[0];
-            } else {
-#pragma unroll
-            for (int nt = 0; nt < NT; nt++) {
-                const int n = 8 * nt + 2 * q;
-                float z0 = acc[mt][nt][2 * half], z1 = acc[mt][nt][2 * half + 1];
-                if (MODE == kSgRelu || MODE == kSgResidual) {
-                    z0 = fmaxf(z0 + a.bias[n], 0.0f);
-                    z1 = fmaxf(z1 + a.bias[n + 1], 0.0f);
-                }
-                if (MODE == kSgResidual && a.aux)
-                    *reinterpret_cast<__nv_bfloat162 *>(&a.aux[p * COUT + n]) = __floats2bfloat162_rn(z0, z1);
-                if (MODE == kSgResidual || MODE == kSgLinearAdd) {
-                    const __nv_bfloat162 rv = *reinterpret_cast<const __nv_bfloat162 *>(&a.res[p * COUT + n]);
-                    z0 += __bfloat162float(rv.x);
-                    z1 += __bfloat162float(rv.y);
-                }
-                *reinterpret_cast<__nv_bfloat162 *>(&a.out[p * COUT + n]) = __floats2bfloat162_rn(z0, z1);
-            }
-            }
-        }
-    }
+    cp_async_wait<0>();
 }
 
 // Weight gradient of a 3x3 conv:
@@ -377,19 +449,34 @@ static SgConvArgs conv_args(const void *in, const void *w, const float *bias, co
     return a;
 }
 
+template <int CIN, int COUT, int MODE>
+static cudaError_t launch_conv_t(const SgConvArgs &a, int total, cudaStream_t s) {
+    constexpr int smem = sg_conv_smem_bytes<CIN, COUT>();
+    auto k = sg_conv_fwd<CIN, COUT, MODE>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int dev = 0, sms = 0, per_sm = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kSgThreads, smem);
+    if (e != cudaSuccess) return e;
+    const int grid = std::max(1, std::min(total, sms * std::max(1, per_sm)));
+    k<<<grid, kSgThreads, smem, s>>>(a, total);
+    return cudaGetLastError();
+}
+
 static fg_status launch_conv(int32_t kind, const SgConvArgs &a, int nb, cudaStream_t s) {
     const long long blocks = (long long)nb * a.tiles_per_img;
     if (blocks > 0x7FFFFFFFll) return set_error(FG_ERR_UNSUPPORTED, "surrogate batch too large");
-    const unsigned grid = (unsigned)blocks;
+    const int total = (int)blocks;
+    cudaError_t e;
     switch (kind) {
-    case FG_SG_CONV_INPUT: sg_conv_fwd<16, 32, kSgRelu><<<grid, kSgThreads, 0, s>>>(a); break;
-    case FG_SG_CONV_RESIDUAL: sg_conv_fwd<32, 32, kSgResidual><<<grid, kSgThreads, 0, s>>>(a); break;
-    case FG_SG_CONV_OUTPUT: sg_conv_fwd<32, 8, kSgOutput><<<grid, kSgThreads, 0, s>>>(a); break;
-    case FG_SG_CONV_DGRAD_RESIDUAL: sg_conv_fwd<32, 32, kSgLinearAdd><<<grid, kSgThreads, 0, s>>>(a); break;
-    case FG_SG_CONV_DGRAD_OUTPUT: sg_conv_fwd<16, 32, kSgLinear><<<grid, kSgThreads, 0, s>>>(a); break;
+    case FG_SG_CONV_INPUT: e = launch_conv_t<16, 32, kSgRelu>(a, total, s); break;
+    case FG_SG_CONV_RESIDUAL: e = launch_conv_t<32, 32, kSgResidual>(a, total, s); break;
+    case FG_SG_CONV_OUTPUT: e = launch_conv_t<32, 8, kSgOutput>(a, total, s); break;
+    case FG_SG_CONV_DGRAD_RESIDUAL: e = launch_conv_t<32, 32, kSgLinearAdd>(a, total, s); break;
+    case FG_SG_CONV_DGRAD_OUTPUT: e = launch_conv_t<16, 32, kSgLinear>(a, total, s); break;
     default: return set_error(FG_ERR_INVALID, "unknown surrogate conv kind");
     }
-    const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FG_OK : cuda_error(e, "surrogate conv launch");
 }
 
