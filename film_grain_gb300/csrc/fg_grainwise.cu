@@ -15,7 +15,7 @@
 //     queue with a ballot, and every full batch of 32 is rasterised grain by grain by the whole warp;
 //   - an offset can put a pixel centre inside a grain's disk only if frac(czx + offx) lies within
 //     radius_out of 1/2 (and likewise for y).  For N <= 256 each lane turns both tests, widened by a
-//     rounding margin and rounded out to 1/64 buckets, into a bitmask over the sample index (two
+//     rounding margin and rounded out to 1/128 buckets, into a bitmask over the sample index (two
 //     lookups per axis in per-tile sparse OR tables), ANDs them, and the set bits -- about 1.2x the
 //     true candidates -- go through the warp's list to stage B.  For larger N the offsets are sorted
 //     by frac(offx), the cyclic interval of the sorted table around frac(1/2 - czx) is flattened over

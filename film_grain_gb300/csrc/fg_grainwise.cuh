@@ -175,13 +175,13 @@ __device__ __forceinline__ void gw_raster_batch(const GwTile &T, unsigned int *m
 
 // ------------------------------------------------------------------ bitmask candidate filter (N <= 256)
 // For N <= 256 the candidate offsets of a grain are found as a bitmask over the sample index k: the
-// unit interval of frac(offset) is cut into 64 buckets, and for each axis a sparse table holds, for
+// unit interval of frac(offset) is cut into 128 buckets, and for each axis a sparse table holds, for
 // every bucket b and level L, the OR of the sample masks of buckets b .. b + 2^L - 1 (cyclic).  The
 // cyclic interval [c - h, c + h] of an axis test, rounded out to whole buckets, is the OR of two table
 // entries; the AND of the x and y masks is a superset of the pairs that pass both of the tests the
 // flattened stage A applies (so of every pair that can set a bit), and those pairs go to stage B.
-constexpr int kGbBuckets = 64;
-constexpr int kGbLevels = 6;     // spans 1 .. 32 buckets; 64 or more is the full mask
+constexpr int kGbBuckets = 128;
+constexpr int kGbLevels = 7;     // spans 1 .. 64 buckets; 128 or more is the full mask
 constexpr int kGbMaxWords = 8;   // N <= 256
 
 __host__ __device__ inline bool grainwise_uses_bits(int n) { return n <= 32 * kGbMaxWords; }
@@ -190,8 +190,8 @@ __host__ __device__ inline bool grainwise_uses_bits(int n) { return n <= 32 * kG
 // to whole buckets, written to m (kAnd = false) or ANDed into it (kAnd = true).
 template <int MW, bool kAnd>
 __device__ __forceinline__ void gb_axis_mask(const unsigned *tab, int W, float c, float h, int n, unsigned (&m)[MW]) {
-    const int blo = __float2int_rd(FG_FMUL(FG_FSUB(c, h), 64.0f));
-    const int bhi = __float2int_rd(FG_FMUL(FG_FADD(c, h), 64.0f));
+    const int blo = __float2int_rd(FG_FMUL(FG_FSUB(c, h), (float)kGbBuckets));
+    const int bhi = __float2int_rd(FG_FMUL(FG_FADD(c, h), (float)kGbBuckets));
     const int len = bhi - blo + 1;
     if (h >= 0.5f || len >= kGbBuckets) {
         if (!kAnd) {
@@ -249,7 +249,7 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
         offk[k] = make_float2(e.y, e.z);
         float fx = FG_FSUB(e.y, floorf(e.y));
         if (!(fx < 1.0f)) fx = 0.0f;  // a tiny negative offset rounds up to 1; cyclically that is 0
-        bk[k] =(unsigned short)((int)FG_FMUL(fx, 64.0f) | ((int)FG_FMUL(e.x, 64.0f) << 8));
+        bk[k] =(unsigned short)((int)FG_FMUL(fx, (float)kGbBuckets) | ((int)FG_FMUL(e.x, (float)kGbBuckets) << 8));
     }
     for (int t = tid; t < region_words; t += kGwThreads) mask[t] = 0u;
     if (tid == 0) *next_px = 0;

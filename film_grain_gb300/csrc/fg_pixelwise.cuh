@@ -214,10 +214,12 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
         const bool use_cnt = (long long)fw * fh <= kPwFootMax;
 
         // ---- staged window of cells
-        const int wi0 = f2i_floor(FG_FDIV(FG_FSUB(X0, a.rm), a.delta)) - 1;
-        const int wi1 = f2i_floor(FG_FDIV(FG_FADD(X1, a.rm), a.delta)) + 1;
-        const int wj0 = f2i_floor(FG_FDIV(FG_FSUB(Y0, a.rm), a.delta)) - 1;
-        const int wj1 = f2i_floor(FG_FDIV(FG_FADD(Y1, a.rm), a.delta)) + 1;
+        // Every owned sample has xg in [X0, X1) and computes its cell range with these same rounded
+        // operations, which are monotone, so its range lies inside [wi0, wi1] x [wj0, wj1].
+        const int wi0 = f2i_floor(FG_FDIV(FG_FSUB(X0, a.rm), a.delta));
+        const int wi1 = f2i_floor(FG_FDIV(FG_FADD(X1, a.rm), a.delta));
+        const int wj0 = f2i_floor(FG_FDIV(FG_FSUB(Y0, a.rm), a.delta));
+        const int wj1 = f2i_floor(FG_FDIV(FG_FADD(Y1, a.rm), a.delta));
         const long long Wc = (long long)wi1 - wi0 + 1, Hc = (long long)wj1 - wj0 + 1;
         const bool window_fits = Wc > 0 && Hc > 0 && Wc <= kPwEdgeMax && Hc <= kPwEdgeMax && Wc * Hc <= kPwCellMax;
         const int nc = window_fits ? (int)(Wc * Hc) : 0;
