@@ -186,6 +186,33 @@ def cpu_pixel_baseline(oracle, planes, wl, threads, rows=None):
 SG_CONV_DRAM_BYTES_PER_PX = 354.6e6 / (3 * 1024 * 1024)
 GRAINWISE_DRAM_BYTES_PER_OUT_PX = 17.94e6 / (1024 * 1024)
 
+PIXELWISE_DRAM_BYTES_PER_OUT_PX = (347.3e6 + 58.8e6) / (4096 * 4096)
+
+# Algorithmic lane-ops of the pixel-wise path (an exact method that hashes every cell once): per cell
+# the cell hash and first uniform (three SplitMix64 finalisers, ~62), per non-empty cell the Knuth
+# continuation (~60), per grain its generation (150 lognormal / 70 const), per sample its point and
+# cell range (~30), and ~8 per disk test, a sample testing the grains of its cell range until the first
+# hit (all of them when uncovered, half on average when covered).  Expectations from the lambda plane.
+PW_COST = dict(cell=62, nonempty=60, grain_lognorm=150, grain_const=70, sample=30, test=8)
+
+
+def pixelwise_lane_ops(lam, wl, derived, out_px):
+    lam = lam.astype(np.float64)
+    d, rm = float(derived.delta), float(derived.rm)
+    h, w = lam.shape
+    cells = (w + 2 * rm) * (h + 2 * rm) / (d * d)
+    nonempty = float(np.sum(1.0 - np.exp(-lam * d * d))) / (d * d)
+    grains = float(lam.sum())
+    samples = float(out_px) * wl["n"]
+    u = 1.0 - np.exp(-lam / float(derived.inv_e_pi_r2))
+    tests = samples * float(np.mean(lam * (2 * rm + d) ** 2 * (1.0 - u / 2)))
+    c_g = PW_COST["grain_lognorm"] if wl["dist"] == "lognorm" else PW_COST["grain_const"]
+    terms = dict(cells=cells, nonempty_cells=nonempty, grains=grains, samples=samples, tests=tests)
+    terms["total"] = (PW_COST["cell"] * cells + PW_COST["nonempty"] * nonempty + c_g * grains +
+                      PW_COST["sample"] * samples + PW_COST["test"] * tests)
+    return terms
+
+
 # Algorithmic lane-ops of the grain-wise path (minimal exact implementation; derivation in the design doc).
 GW_COST = dict(grain_lognorm=150, grain_const=70, x_pair=10, y_pair=8, hit=12, out_base=3, out_word=2)
 
@@ -673,6 +700,17 @@ def main():
                                              "(profiles/grainwise_kernel_grain_rgb_512_ncu.md), scaled by output pixels",
                             "kernel": "grainwise_persistent_kernel (launch_ms: the whole plane)", "launch_ms": launch_ms,
                             "lane_ops_per_launch": ops, "counts": counts,
+                            "peak_basis": f"{sm_count} SMs x 128 lanes x {f_mhz:.0f} MHz (sampled)"}
+    if wl["algo"] == "pixel":
+        ops = [pixelwise_lane_ops(lh, wl, derived, ow * oh) for lh in lam_host]
+        ach = sum(o["total"] / (ms / 1e3) for o, ms in zip(ops, launch_ms)) / len(ops)
+        line["roofline"] = {"bound": "sm_issue", "achieved": ach / 1e12, "peak": peak / 1e12, "unit": "Tlane-op/s",
+                            "frac": ach / peak,
+                            "traffic": PIXELWISE_DRAM_BYTES_PER_OUT_PX * ow * oh,
+                            "traffic_basis": "ncu dram bytes of the pixel_rgb_4096 launch "
+                                             "(profiles/pixelwise_kernel_pixel_rgb_4096_ncu.md), scaled by output pixels",
+                            "kernel": "pixelwise_kernel (launch_ms: the whole plane)", "launch_ms": launch_ms,
+                            "lane_ops_per_launch": [o["total"] for o in ops], "model_terms": ops[0],
                             "peak_basis": f"{sm_count} SMs x 128 lanes x {f_mhz:.0f} MHz (sampled)"}
     print(json.dumps(line), flush=True)
     if dist:
