@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(512, 2) batch_persistent_kernel(const BatchIma
         }
         __syncthreads();
         if (threadIdx.x == 0) s_image = w.image;
-        if (s_img.algo == FG_ALGO_PIXEL) pixelwise_block(s_img.pa, w.x, w.y, smem_raw);
+        if (s_img.algo == FG_ALGO_PIXEL) pixelwise_block<PwFat>(s_img.pa, w.x, w.y, smem_raw);
         else if (s_img.small) grainwise_tile<true>(s_img.ga, w.x, w.y, smem_raw);
         else grainwise_tile<false>(s_img.ga, w.x, w.y, smem_raw);
         __syncthreads();

@@ -117,16 +117,31 @@ PixelwiseArgs pixelwise_args(const fg_params &p, const fg_derived &d, const PwPl
     return a;
 }
 
+// Stream-ordered device buffer that frees itself.
+struct DevBuf {
+    void *p = nullptr;
+    cudaStream_t s = nullptr;
+    cudaError_t alloc(size_t bytes, cudaStream_t st) {
+        s = st;
+        return cudaMallocAsync(&p, bytes ? bytes : 16, st);
+    }
+    ~DevBuf() {
+        if (p) cudaFreeAsync(p, s);
+    }
+};
+
 fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_derived &d, const float *h_offs_in,
                             const float *d_offs_in, float *d_out, CellParam *d_cells, unsigned long long *d_diag,
-                            const EpilogueArgs *colour, cudaStream_t s) {
+                            const EpilogueArgs *colour, cudaStream_t s, bool may_allocate) {
     const int in_w = (int)d.input_width, in_h = (int)d.input_height;
     const int out_w = (int)d.output_width, out_h = (int)d.output_height;
     const PwPlan pl = plan_pixelwise(p, d, h_offs_in, 4);
     FG_CUDA(launch_cell_params(d_lam, in_w, in_h, d.delta, d_cells, s), "cell params");
     FG_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * (size_t)out_w * out_h, s), "memset");
     const PixelwiseArgs a = pixelwise_args(p, d, pl, d_lam, d_cells, d_offs_in, d_out, d_diag);
-    FG_CUDA(launch_pixelwise(a, pl.nby, pixelwise_smem_bytes(), s), "pixelwise kernel");
+    DevBuf defer;  // the lean pass's list of deferred root blocks (none without allocation: fat CTAs only)
+    if (may_allocate) FG_CUDA(defer.alloc((1 + (size_t)pl.nbx * pl.nby) * sizeof(int), s), "alloc defer list");
+    FG_CUDA(launch_pixelwise(a, pl.nby, static_cast<int *>(defer.p), s), "pixelwise kernel");
     EpilogueArgs e;
     if (colour) e = *colour;
     else std::memset(&e, 0, sizeof e);
@@ -214,19 +229,6 @@ GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const floa
 size_t grainwise_mask_bytes(const fg_params &p, const fg_derived &d) {
     return (size_t)d.output_width * d.output_height * ((p.n_samples + 31) / 32) * sizeof(unsigned int);
 }
-
-// Stream-ordered device buffer that frees itself.
-struct DevBuf {
-    void *p = nullptr;
-    cudaStream_t s = nullptr;
-    cudaError_t alloc(size_t bytes, cudaStream_t st) {
-        s = st;
-        return cudaMallocAsync(&p, bytes ? bytes : 16, st);
-    }
-    ~DevBuf() {
-        if (p) cudaFreeAsync(p, s);
-    }
-};
 
 fg_status enqueue_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
     if (grainwise_smem_bytes(a) > 200 * 1024)

@@ -17,9 +17,18 @@ struct __align__(16) CellParam {
 };
 
 // Shared-memory capacities of the pixel-wise tile kernel.
-constexpr int kPwThreads = 512;
 constexpr int kPwCellMax = 8192;   // staged window cells
-constexpr int kPwGrainMax = 4096;  // staged grains (16 B each)
+// Shared-memory configurations of the pixel-wise block: lean CTAs (256 threads, 4 per SM) take every
+// block first and defer the dense ones; fat CTAs (512 threads, 2 per SM) take the deferred blocks
+// (and every block of the batched and allocation-free paths).
+struct PwLean {
+    static constexpr int kThreads = 256, kCtasPerSm = 4, kGrainMax = 1024, kListMax = 2048;
+    static constexpr bool kDefers = true;
+};
+struct PwFat {
+    static constexpr int kThreads = 512, kCtasPerSm = 2, kGrainMax = 4096, kListMax = 8192;
+    static constexpr bool kDefers = false;
+};
 constexpr int kPwEdgeMax = 128;    // window cells per axis
 constexpr int kPwKChunk = 256;     // offsets per sample-assignment chunk
 constexpr int kPwFootMax = 1024;   // per-block output-pixel counters
@@ -41,6 +50,7 @@ struct PixelwiseArgs {
     int lognorm;
     float radius_mean;
     double log_mu, log_sigma;
+    int *defer;                 // lean pass: [0] count, [1..] deferred root blocks (nbx-major); else null
 };
 
 constexpr int kGwBucketCount = 256;  // bucket index over the frac(offx)-sorted offsets
@@ -87,8 +97,10 @@ struct EpilogueArgs {
 };
 
 cudaError_t launch_cell_params(const float *lam, int in_w, int in_h, float delta, CellParam *cells, cudaStream_t s);
-cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, size_t smem, cudaStream_t s);
-size_t pixelwise_smem_bytes();
+// defer: null (fat CTAs over every block) or a buffer of 1 + nbx*nby ints (lean pass, then fat CTAs
+// over the deferred blocks).
+cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, cudaStream_t s);
+size_t pixelwise_smem_bytes();  // the fat configuration (the batched kernel's pixel-wise items)
 cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s);
 size_t grainwise_smem_bytes(const GrainwiseArgs &a);
 int grainwise_tile_count(const GrainwiseArgs &a);

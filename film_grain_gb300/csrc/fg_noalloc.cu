@@ -88,7 +88,8 @@ extern "C" FG_API fg_status fg_render_pixelwise_noalloc(const float *d_lambda, c
     if (e != cudaSuccess) return cuda_error(e, "offsets H2D");
     e = cudaMemsetAsync(diag, 0, kNaDiagBytes, s);
     if (e != cudaSuccess) return cuda_error(e, "clear counters");
-    st = enqueue_pixelwise(d_lambda, *params, *derived, offsets_input, offs, d_out, cells, diag, nullptr, s);
+    st = enqueue_pixelwise(d_lambda, *params, *derived, offsets_input, offs, d_out, cells, diag, nullptr, s,
+                           /*may_allocate=*/false);
     if (st == FG_OK) clear_error();
     return st;
 }

@@ -19,6 +19,8 @@
 // window holds more grains than shared memory splits into quadrants (up to kPwMaxLevel levels);
 // samples whose cell range leaves the staged window (never expected) and leaf blocks that still
 // overflow fall back to the reference's per-sample regeneration, which is exact too.
+#include <algorithm>
+
 #include "fg_kernels.cuh"
 #include "fg_rng.cuh"
 #include "fg_color.cuh"
@@ -58,23 +60,60 @@ cudaError_t launch_cell_params(const float *lam, int in_w, int in_h, float delta
     return cudaGetLastError();
 }
 
-size_t pixelwise_smem_bytes() { return sizeof(PwShared); }
+size_t pixelwise_smem_bytes() { return sizeof(PwShared<PwFat>); }
 
-__global__ void __launch_bounds__(kPwThreads, 2) pixelwise_kernel(const __grid_constant__ PixelwiseArgs a) {
+// One CTA per root block (block-grid row-major from (bx0, by0)).
+template <class C>
+__global__ void __launch_bounds__(C::kThreads, C::kCtasPerSm) pixelwise_kernel(const __grid_constant__ PixelwiseArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    pixelwise_block(a, a.bx0 + (int)(blockIdx.x % (unsigned)a.nbx), a.by0 + (int)(blockIdx.x / (unsigned)a.nbx), smem_raw);
+    pixelwise_block<C>(a, a.bx0 + (int)(blockIdx.x % (unsigned)a.nbx), a.by0 + (int)(blockIdx.x / (unsigned)a.nbx),
+                       smem_raw);
 }
 
-cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, size_t smem, cudaStream_t s) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(pixelwise_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
+// The root blocks the lean pass deferred, in fat CTAs (persistent over the list).
+__global__ void __launch_bounds__(PwFat::kThreads, PwFat::kCtasPerSm)
+    pixelwise_deferred_kernel(const __grid_constant__ PixelwiseArgs a, const int *__restrict__ defer) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = defer[0];
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        const int id = defer[1 + i];
+        pixelwise_block<PwFat>(a, a.bx0 + id % a.nbx, a.by0 + id / a.nbx, smem_raw);
+        __syncthreads();
     }
-    long long nblocks = (long long)a.nbx * nby;
+}
+
+template <class K>
+static cudaError_t set_smem(K k, size_t smem) {
+    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, cudaStream_t s) {
+    const size_t lean_smem = sizeof(PwShared<PwLean>), fat_smem = sizeof(PwShared<PwFat>);
+    cudaError_t e = set_smem(pixelwise_kernel<PwLean>, lean_smem);
+    if (e == cudaSuccess) e = set_smem(pixelwise_kernel<PwFat>, fat_smem);
+    if (e == cudaSuccess) e = set_smem(pixelwise_deferred_kernel, fat_smem);
+    if (e != cudaSuccess) return e;
+    const long long nblocks = (long long)a.nbx * nby;
     if (nblocks <= 0) return cudaSuccess;
-    pixelwise_kernel<<<(unsigned)nblocks, kPwThreads, smem, s>>>(a);
+    if (!defer) {
+        pixelwise_kernel<PwFat><<<(unsigned)nblocks, PwFat::kThreads, fat_smem, s>>>(a);
+        return cudaGetLastError();
+    }
+    e = cudaMemsetAsync(defer, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    PixelwiseArgs lean = a;
+    lean.defer = defer;
+    pixelwise_kernel<PwLean><<<(unsigned)nblocks, PwLean::kThreads, lean_smem, s>>>(lean);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    PixelwiseArgs fat = a;
+    fat.defer = nullptr;
+    const long long grid = std::min<long long>(nblocks, (long long)std::max(1, sms) * PwFat::kCtasPerSm);
+    pixelwise_deferred_kernel<<<(unsigned)grid, PwFat::kThreads, fat_smem, s>>>(fat, defer);
     return cudaGetLastError();
 }
 

@@ -103,9 +103,9 @@ static __device__ bool eval_regen(const PixelwiseArgs &a, const UniformF32 &U, f
     return false;
 }
 
-// Block-wide exclusive scan of one int per thread (blockDim.x == kPwThreads).
+// Block-wide exclusive scan of one int per thread (any blockDim.x that is a multiple of 32, <= 1024).
 __device__ __forceinline__ int block_excl_scan(int v, int *wsum, int *total) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     int x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -115,15 +115,15 @@ __device__ __forceinline__ int block_excl_scan(int v, int *wsum, int *total) {
     if (lane == 31) wsum[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        int w = (lane < (kPwThreads / 32)) ? wsum[lane] : 0;
+        int w = (lane < nwarps) ? wsum[lane] : 0;
         int t = w;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             int y = __shfl_up_sync(0xffffffffu, t, o);
             if (lane >= o) t += y;
         }
-        if (lane < (kPwThreads / 32)) wsum[lane] = t - w;
-        if (lane == (kPwThreads / 32) - 1) wsum[32] = t;
+        if (lane < nwarps) wsum[lane] = t - w;
+        if (lane == nwarps - 1) wsum[32] = t;
     }
     __syncthreads();
     int r = wsum[warp] + x - v;
@@ -133,10 +133,11 @@ __device__ __forceinline__ int block_excl_scan(int v, int *wsum, int *total) {
 }
 
 // ------------------------------------------------------------------ shared-memory layout
+template <class C>
 struct PwShared {
-    float4 grains[kPwGrainMax];
+    float4 grains[C::kGrainMax];
     unsigned short pre[kPwCellMax + 8];   // counts, then exclusive prefix (row-major window cells)
-    unsigned short list[kPwCellMax];      // non-empty cells
+    unsigned short list[C::kListMax];     // non-empty cells
     int colix[kPwEdgeMax], rowiy[kPwEdgeMax];
     int4 rect[kPwKChunk];                 // owned pixel rectangle per offset: xa, xe, ya, ye
     int spre[kPwKChunk + 1];
@@ -149,13 +150,24 @@ struct PwShared {
     int flags;                            // bit0: overflow, bit1: leaf slow path
     int fx0, fx1, fy0, fy1;               // owned-pixel footprint
     int nsamples;
+    float est_grains, est_cells;          // lean pass: expected grains / non-empty cells of the window
 };
 
-// One root block of the pixel-wise tile kernel (all threads of the CTA; `smem_raw` holds PwShared).
+// Lean pass: hand the root block to the fat pass (thread 0).
+__device__ __forceinline__ void pw_defer(const PixelwiseArgs &a, int root_x, int root_y) {
+    const int slot = atomicAdd(a.defer, 1);
+    a.defer[1 + slot] = (root_y - a.by0) * a.nbx + (root_x - a.bx0);
+}
+
+// One root block of the pixel-wise tile kernel (all threads of the CTA; `smem_raw` holds PwShared<C>).
+// With C::kDefers and a.defer set, a root block whose window is expected to overflow the lean buffers
+// (or does overflow them) is appended to a.defer instead of being split, and produces no output here.
+template <class C>
 __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root_x, int root_y,
                                                 unsigned char *smem_raw) {
-    PwShared &S = *reinterpret_cast<PwShared *>(smem_raw);
-    const int tid = threadIdx.x;
+    PwShared<C> &S = *reinterpret_cast<PwShared<C> *>(smem_raw);
+    const int tid = threadIdx.x, nthreads = blockDim.x;
+    const bool lean = C::kDefers && a.defer != nullptr;
     const UniformF32 U = uniform_f32_new(0.0f, a.delta);
 
     if (tid == 0) {
@@ -176,6 +188,46 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
         const float X0 = FG_FMUL((float)sbx, bs), X1 = FG_FMUL((float)(sbx + 1), bs);
         const float Y0 = FG_FMUL((float)sby, bs), Y1 = FG_FMUL((float)(sby + 1), bs);
 
+        if (lean && level == 0) {
+            // expected grains and non-empty cells of the window: lambda integrated over its rectangle
+            // (a cell takes the lambda of the pixel containing its origin; edge pixels extend outwards)
+            const float wx0 = FG_FMUL((float)(f2i_floor(FG_FDIV(FG_FSUB(X0, a.rm), a.delta))), a.delta);
+            const float wx1 = FG_FMUL((float)(f2i_floor(FG_FDIV(FG_FADD(X1, a.rm), a.delta)) + 1), a.delta);
+            const float wy0 = FG_FMUL((float)(f2i_floor(FG_FDIV(FG_FSUB(Y0, a.rm), a.delta))), a.delta);
+            const float wy1 = FG_FMUL((float)(f2i_floor(FG_FDIV(FG_FADD(Y1, a.rm), a.delta)) + 1), a.delta);
+            const int px0 = (int)floorf(wx0), px1 = (int)floorf(wx1), py0 = (int)floorf(wy0), py1 = (int)floorf(wy1);
+            const int nx = px1 - px0 + 1, npx = nx * (py1 - py0 + 1);
+            if (tid == 0) { S.est_grains = 0.0f; S.est_cells = 0.0f; }
+            __syncthreads();
+            float g = 0.0f, c = 0.0f;
+            const float inv_cell = 1.0f / (a.delta * a.delta);
+            for (int t = tid; t < npx; t += nthreads) {
+                const int px = px0 + t % nx, py = py0 + t / nx;
+                const float ox = fminf((float)(px + 1), wx1) - fmaxf((float)px, wx0);
+                const float oy = fminf((float)(py + 1), wy1) - fmaxf((float)py, wy0);
+                if (ox > 0.0f && oy > 0.0f) {
+                    const int cx = min(max(px, 0), a.in_w - 1), cy = min(max(py, 0), a.in_h - 1);
+                    const float lam = a.lam[(long long)cy * a.in_w + cx];
+                    g += lam * ox * oy;
+                    c += (1.0f - __expf(-lam * a.delta * a.delta)) * ox * oy * inv_cell;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                g += __shfl_xor_sync(0xffffffffu, g, o);
+                c += __shfl_xor_sync(0xffffffffu, c, o);
+            }
+            if ((tid & 31) == 0 && (g > 0.0f || c > 0.0f)) {
+                atomicAdd(&S.est_grains, g);
+                atomicAdd(&S.est_cells, c);
+            }
+            __syncthreads();
+            if (S.est_grains > 0.75f * (float)C::kGrainMax || S.est_cells > 0.75f * (float)C::kListMax) {
+                if (tid == 0) pw_defer(a, root_x, root_y);
+                continue;  // loop head syncs
+            }
+        }
+
         // ---- ownership: rectangles per offset, sample total and pixel footprint
         if (tid == 0) { S.fx0 = 0x7fffffff; S.fx1 = -1; S.fy0 = 0x7fffffff; S.fy1 = -1; S.nsamples = 0; }
         __syncthreads();
@@ -183,7 +235,7 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
         const bool one_chunk = a.n <= kPwKChunk;
         {
             int lx0 = 0x7fffffff, lx1 = -1, ly0 = 0x7fffffff, ly1 = -1, ns = 0;
-            for (int k = tid; k < a.n; k += kPwThreads) {
+            for (int k = tid; k < a.n; k += nthreads) {
                 float2 o = a.offs[k];
                 int xa = first_at_least(X0, a.out_w, a.inv_zoom, a.zoom, o.x);
                 int xe = first_at_least(X1, a.out_w, a.inv_zoom, a.zoom, o.x);
@@ -225,14 +277,14 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
         const int nc = window_fits ? (int)(Wc * Hc) : 0;
 
         if (use_cnt)
-            for (int t = tid; t < fw * fh; t += kPwThreads) S.cnt[t] = 0u;
+            for (int t = tid; t < fw * fh; t += nthreads) S.cnt[t] = 0u;
         if (tid == 0) { S.nlist = 0; S.flags = 0; }
         if (window_fits) {
-            for (int t = tid; t < Wc; t += kPwThreads) {
+            for (int t = tid; t < Wc; t += nthreads) {
                 long long ix = (long long)floorf(FG_FMUL((float)(wi0 + t), a.delta));
                 S.colix[t] = (int)(ix < 0 ? 0 : (ix > a.in_w - 1 ? a.in_w - 1 : ix));
             }
-            for (int t = tid; t < Hc; t += kPwThreads) {
+            for (int t = tid; t < Hc; t += nthreads) {
                 long long iy = (long long)floorf(FG_FMUL((float)(wj0 + t), a.delta));
                 S.rowiy[t] = (int)(iy < 0 ? 0 : (iy > a.in_h - 1 ? a.in_h - 1 : iy));
             }
@@ -247,7 +299,7 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
             // Poisson set-up along the run.  Empty cells get count 0; the others join the list
             // (one shared atomic per warp step) and get their count in A2.
             {
-                const int per = (nc + kPwThreads - 1) / kPwThreads;
+                const int per = (nc + nthreads - 1) / nthreads;
                 const int c0 = tid * per, c1 = min(nc, c0 + per);
                 const int lane = tid & 31;
                 int ci = c0 / (int)Hc, cj = c0 % (int)Hc;
@@ -284,15 +336,17 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
                         int slot0 = 0;
                         if (lane == __ffs(nb) - 1) slot0 = atomicAdd(&S.nlist, __popc(nb));
                         slot0 = __shfl_sync(0xffffffffu, slot0, __ffs(nb) - 1);
-                        if (nonempty) S.list[slot0 + __popc(nb & ((1u << lane) - 1u))] = (unsigned short)rc;
+                        const int idx = slot0 + __popc(nb & ((1u << lane) - 1u));
+                        if (nonempty && idx < C::kListMax) S.list[idx] = (unsigned short)rc;
                     }
                 }
             }
             __syncthreads();
+            const bool list_overflow = S.nlist > C::kListMax;  // handled like a grain overflow below
             // ---- pass A2: the grain counts of the non-empty cells, one cell per thread
-            {
+            if (!list_overflow) {
                 const int nl = S.nlist;
-                for (int t = tid; t < nl; t += kPwThreads) {
+                for (int t = tid; t < nl; t += nthreads) {
                     const int rc = S.list[t];
                     const int ci = rc % (int)Wc, cj = rc / (int)Wc;
                     const CellParam cp = a.cells[(long long)S.rowiy[cj] * a.in_w + S.colix[ci]];
@@ -304,14 +358,16 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
             }
             __syncthreads();
             // ---- exclusive prefix over the counts (each thread owns a contiguous run)
-            {
-                const int per = (nc + kPwThreads - 1) / kPwThreads;
+            if (list_overflow) {
+                if (tid == 0) S.flags |= 1;
+            } else {
+                const int per = (nc + nthreads - 1) / nthreads;
                 const int b = tid * per, e = min(nc, b + per);
                 int local = 0;
                 for (int c = b; c < e; c++) local += S.pre[c];
                 int total;
                 int run = block_excl_scan(local, S.wsum, &total);
-                if (total <= kPwGrainMax) {
+                if (total <= C::kGrainMax) {
                     for (int c = b; c < e; c++) {
                         int q = S.pre[c];
                         S.pre[c] = (unsigned short)run;
@@ -319,13 +375,17 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
                     }
                 }
                 if (tid == 0) {
-                    S.pre[nc] = (unsigned short)(total <= kPwGrainMax ? total : 0);
+                    S.pre[nc] = (unsigned short)(total <= C::kGrainMax ? total : 0);
                     S.total = total;
-                    if (total > kPwGrainMax) S.flags |= 1;
+                    if (total > C::kGrainMax) S.flags |= 1;
                 }
             }
             __syncthreads();
             if (S.flags & 1) {
+                if (lean && level == 0) {  // the fat pass takes this block whole
+                    if (tid == 0) pw_defer(a, root_x, root_y);
+                    continue;  // loop head syncs
+                }
                 if (level < kPwMaxLevel) {
                     if (tid == 0) {
                         atomicAdd(&a.diag[2], 1ull);
@@ -347,7 +407,7 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
         if (staged) {
             // ---- pass B: regenerate the non-empty cells' grains into their CSR slots
             const int nl = S.nlist;
-            for (int t = tid; t < nl; t += kPwThreads) {
+            for (int t = tid; t < nl; t += nthreads) {
                 const int c = S.list[t];
                 const int ci = c % (int)Wc, cj = c / (int)Wc;
                 const int i = wi0 + ci, j = wj0 + cj;
@@ -399,7 +459,7 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
             if (tid < kPwKChunk) S.spre[tid] = off;
             if (tid == 0) S.spre[kPwKChunk] = tot;
             __syncthreads();
-            for (int s = tid; s < tot; s += kPwThreads) {
+            for (int s = tid; s < tot; s += nthreads) {
                 int lo = 0, hi = kn - 1;  // last kk with spre[kk] <= s
                 while (lo < hi) {
                     int mid = (lo + hi + 1) >> 1;
@@ -450,7 +510,7 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
 
         // ---- flush per-pixel counts
         if (use_cnt) {
-            for (int t = tid; t < fw * fh; t += kPwThreads) {
+            for (int t = tid; t < fw * fh; t += nthreads) {
                 unsigned c = S.cnt[t];
                 if (c) atomicAdd(&a.out[(long long)(fy0 + t / fw) * a.out_w + (fx0 + t % fw)], (float)c);
             }
