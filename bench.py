@@ -183,10 +183,10 @@ def cpu_pixel_baseline(oracle, planes, wl, threads, rows=None):
 # DRAM bytes per launch measured by ncu on the profiling cases (profiles/*_ncu.md), per unit of work:
 # sg_conv_fwd<32,32,residual>: 354.6 MB read+write for 3 x 1024^2 px; grainwise_kernel: 17.94 MB for a
 # 1024^2-pixel output plane (the lambda plane plus the sample-mask lines that miss L2).
-SG_CONV_DRAM_BYTES_PER_PX = 354.6e6 / (3 * 1024 * 1024)
-GRAINWISE_DRAM_BYTES_PER_OUT_PX = 17.94e6 / (1024 * 1024)
+SG_CONV_DRAM_BYTES_PER_PX = 358.6e6 / (3 * 1024 * 1024)
+GRAINWISE_DRAM_BYTES_PER_OUT_PX = 18.25e6 / (1024 * 1024)
 
-PIXELWISE_DRAM_BYTES_PER_OUT_PX = (347.3e6 + 58.8e6) / (4096 * 4096)
+PIXELWISE_DRAM_BYTES_PER_OUT_PX = (399.3e6 + 59.4e6) / (4096 * 4096)
 
 # Algorithmic lane-ops of the pixel-wise path (an exact method that hashes every cell once): per cell
 # the cell hash and first uniform (three SplitMix64 finalisers, ~62), per non-empty cell the Knuth
