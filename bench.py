@@ -181,7 +181,7 @@ def cpu_pixel_baseline(oracle, planes, wl, threads, rows=None):
 
 
 # DRAM bytes per launch measured by ncu on the profiling cases (profiles/*_ncu.md), per unit of work:
-# sg_conv_fwd<32,32,residual>: 354.6 MB read+write for 3 x 1024^2 px; grainwise_kernel: 17.94 MB for a
+# sg_conv_fwd<32,32,residual>: 358.6 MB read+write for 3 x 1024^2 px; grainwise kernel: 18.25 MB for a
 # 1024^2-pixel output plane (the lambda plane plus the sample-mask lines that miss L2).
 SG_CONV_DRAM_BYTES_PER_PX = 358.6e6 / (3 * 1024 * 1024)
 GRAINWISE_DRAM_BYTES_PER_OUT_PX = 18.25e6 / (1024 * 1024)

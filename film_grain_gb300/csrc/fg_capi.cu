@@ -140,7 +140,7 @@ fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_der
     FG_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * (size_t)out_w * out_h, s), "memset");
     const PixelwiseArgs a = pixelwise_args(p, d, pl, d_lam, d_cells, d_offs_in, d_out, d_diag);
     DevBuf defer;  // the lean pass's list of deferred root blocks (none without allocation: fat CTAs only)
-    if (may_allocate) FG_CUDA(defer.alloc((1 + (size_t)pl.nbx * pl.nby) * sizeof(int), s), "alloc defer list");
+    if (may_allocate) FG_CUDA(defer.alloc((2 + (size_t)pl.nbx * pl.nby) * sizeof(int), s), "alloc defer list");
     FG_CUDA(launch_pixelwise(a, pl.nby, static_cast<int *>(defer.p), s), "pixelwise kernel");
     EpilogueArgs e;
     if (colour) e = *colour;

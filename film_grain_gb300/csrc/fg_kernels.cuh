@@ -97,7 +97,7 @@ struct EpilogueArgs {
 };
 
 cudaError_t launch_cell_params(const float *lam, int in_w, int in_h, float delta, CellParam *cells, cudaStream_t s);
-// defer: null (fat CTAs over every block) or a buffer of 1 + nbx*nby ints (lean pass, then fat CTAs
+// defer: null (fat CTAs over every block) or a buffer of 2 + nbx*nby ints (lean pass, then fat CTAs
 // over the deferred blocks).
 cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, cudaStream_t s);
 size_t pixelwise_smem_bytes();  // the fat configuration (the batched kernel's pixel-wise items)

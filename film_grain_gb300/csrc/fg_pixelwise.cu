@@ -70,13 +70,21 @@ __global__ void __launch_bounds__(C::kThreads, C::kCtasPerSm) pixelwise_kernel(c
                        smem_raw);
 }
 
-// The root blocks the lean pass deferred, in fat CTAs (persistent over the list).
+// The root blocks the lean pass deferred, in fat CTAs: persistent, each CTA taking the next listed
+// block from the counter defer[-1] (the word before the list's count).
 __global__ void __launch_bounds__(PwFat::kThreads, PwFat::kCtasPerSm)
-    pixelwise_deferred_kernel(const __grid_constant__ PixelwiseArgs a, const int *__restrict__ defer) {
+    pixelwise_deferred_kernel(const __grid_constant__ PixelwiseArgs a, int *__restrict__ defer) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_id;
     const int n = defer[0];
-    for (int i = blockIdx.x; i < n; i += gridDim.x) {
-        const int id = defer[1 + i];
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int i = atomicAdd(defer - 1, 1);
+            s_id = i < n ? defer[1 + i] : -1;
+        }
+        __syncthreads();
+        const int id = s_id;
+        if (id < 0) break;
         pixelwise_block<PwFat>(a, a.bx0 + id % a.nbx, a.by0 + id / a.nbx, smem_raw);
         __syncthreads();
     }
@@ -99,10 +107,10 @@ cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, cudaSt
         pixelwise_kernel<PwFat><<<(unsigned)nblocks, PwFat::kThreads, fat_smem, s>>>(a);
         return cudaGetLastError();
     }
-    e = cudaMemsetAsync(defer, 0, sizeof(int), s);
+    e = cudaMemsetAsync(defer, 0, 2 * sizeof(int), s);  // [0] the fat pass's counter, [1] the list's count
     if (e != cudaSuccess) return e;
     PixelwiseArgs lean = a;
-    lean.defer = defer;
+    lean.defer = defer + 1;
     pixelwise_kernel<PwLean><<<(unsigned)nblocks, PwLean::kThreads, lean_smem, s>>>(lean);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -113,7 +121,7 @@ cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, cudaSt
     PixelwiseArgs fat = a;
     fat.defer = nullptr;
     const long long grid = std::min<long long>(nblocks, (long long)std::max(1, sms) * PwFat::kCtasPerSm);
-    pixelwise_deferred_kernel<<<(unsigned)grid, PwFat::kThreads, fat_smem, s>>>(fat, defer);
+    pixelwise_deferred_kernel<<<(unsigned)grid, PwFat::kThreads, fat_smem, s>>>(fat, defer + 1);
     return cudaGetLastError();
 }
 
