@@ -4,12 +4,16 @@
 // per-image entry points render them).  Creating a batch plans every image (launch plans as in
 // fg_capi.cu, under the batch's tuning), cuts the work into items -- pixel-wise root blocks and
 // grain-wise input tiles -- and sorts them by estimated cost, largest first; it then captures one
-// CUDA graph of three kernels:
+// CUDA graph of four kernels:
 //   1. a segmented kernel that zeroes the accumulators (pixel-wise output planes, grain-wise sample
 //      masks, the work counter) and builds the pixel-wise images' cell tables;
-//   2. the persistent kernel: 2 CTAs per SM pull items from an atomic counter and run the same tile
-//      code as the per-image kernels (fg_pixelwise.cuh / fg_grainwise.cuh), so results are identical;
-//   3. a segmented epilogue kernel: pixel-wise count * (1/N), grain-wise popcount * (1/N).
+//   2. a lean persistent kernel (256 threads, 4 CTAs per SM) over the pixel-wise root blocks, which
+//      leaves blocks too dense for its shared-memory buffers to the next kernel (as the per-image
+//      lean pass does);
+//   3. the persistent kernel: 2 CTAs per SM pull the deferred pixel-wise blocks, then the grain-wise
+//      tiles, from an atomic counter and run the same tile code as the per-image kernels
+//      (fg_pixelwise.cuh / fg_grainwise.cuh), so results are identical;
+//   4. a segmented epilogue kernel: pixel-wise count * (1/N), grain-wise popcount * (1/N).
 // fg_batch_run replays the graph.  fg_batch_autotune times candidate tunings (grain-wise tile mask
 // budget, pixel-wise block edge, CTAs per SM) on the batch itself and returns the fastest.
 #include <algorithm>
@@ -95,20 +99,53 @@ __global__ void batch_segments_kernel(const Segment *__restrict__ segs, const Ch
     }
 }
 
+// counters: [0] the lean kernel's next item, [1] the persistent kernel's next item, [2] deferred items.
+
+// Pixel-wise items in lean CTAs (256 threads, 4 per SM); the root blocks they leave to fat CTAs are
+// appended to `deferred` for the persistent kernel.
+__global__ void __launch_bounds__(PwLean::kThreads, PwLean::kCtasPerSm)
+    batch_lean_kernel(const BatchImage *__restrict__ images, const BatchItem *__restrict__ items, int n_items,
+                      int *counters, BatchItem *__restrict__ deferred) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_item;
+    __shared__ int s_image;
+    __shared__ __align__(16) PixelwiseArgs s_pa;
+    if (threadIdx.x == 0) s_image = -1;
+    while (true) {
+        if (threadIdx.x == 0) s_item = atomicAdd(&counters[0], 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= n_items) break;
+        const BatchItem w = items[it];
+        if (w.image != s_image) {
+            const int *src = reinterpret_cast<const int *>(&images[w.image].pa);
+            int *dst = reinterpret_cast<int *>(&s_pa);
+            for (int k = threadIdx.x; k < (int)(sizeof(PixelwiseArgs) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_image = w.image;
+        const bool left = pixelwise_block<PwLean>(s_pa, w.x, w.y, smem_raw, true);
+        if (left && threadIdx.x == 0) deferred[atomicAdd(&counters[2], 1)] = w;
+        __syncthreads();
+    }
+}
+
+// The deferred pixel-wise blocks first (the densest), then the grain-wise tiles.
 __global__ void __launch_bounds__(512, 2) batch_persistent_kernel(const BatchImage *__restrict__ images,
                                                                   const BatchItem *__restrict__ items, int n_items,
-                                                                  int *counter) {
+                                                                  int *counters, const BatchItem *__restrict__ deferred) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
     __shared__ int s_image;
     __shared__ __align__(16) BatchImage s_img;
     if (threadIdx.x == 0) s_image = -1;
+    const int nd = counters[2];
     while (true) {
-        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+        if (threadIdx.x == 0) s_item = atomicAdd(&counters[1], 1);
         __syncthreads();
         const int it = s_item;
-        if (it >= n_items) break;
-        const BatchItem w = items[it];
+        if (it >= nd + n_items) break;
+        const BatchItem w = it < nd ? deferred[it] : items[it - nd];
         if (w.image != s_image) {  // load the image's descriptor into shared memory
             const int *src = reinterpret_cast<const int *>(&images[w.image]);
             int *dst = reinterpret_cast<int *>(&s_img);
@@ -132,9 +169,14 @@ struct fg_batch {
     fg_batch_tuning tuning{};
     std::vector<void *> owned;  // device allocations (freed on destroy)
     BatchImage *d_images = nullptr;
-    BatchItem *d_items = nullptr;
+    BatchItem *d_items = nullptr;     // grain-wise tiles, heaviest first
     int n_items = 0;
-    int *d_counter = nullptr;
+    BatchItem *d_px_items = nullptr;  // pixel-wise root blocks, heaviest first (the lean kernel's list)
+    int n_px_items = 0;
+    BatchItem *d_deferred = nullptr;  // pixel-wise blocks the lean kernel leaves to fat CTAs
+    int *d_counter = nullptr;         // [0] lean next, [1] persistent next, [2] deferred count
+    int lean_grid = 0;
+    size_t lean_smem = 0;
     Segment *d_segs = nullptr;
     Chunk *d_pre_chunks = nullptr, *d_post_chunks = nullptr;
     int n_pre_chunks = 0, n_post_chunks = 0;
@@ -177,7 +219,7 @@ static void add_chunks(std::vector<Chunk> &chunks, int seg, long long n) {
 
 fg_batch_tuning default_tuning() {
     fg_batch_tuning t;
-    t.grain_mask_words = 16384;
+    t.grain_mask_words = 8192;
     t.pixel_max_block_log2 = 4;
     t.ctas_per_sm = 2;
     return t;
@@ -193,7 +235,7 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
         double cost;
         BatchItem it;
     };
-    std::vector<CostItem> work;
+    std::vector<CostItem> work, px_work;
     std::vector<Segment> segs;
     std::vector<Chunk> pre, post;
     size_t smem = pixelwise_smem_bytes();
@@ -206,7 +248,7 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
         cudaError_t e_ = (call);                                   \
         if (e_ != cudaSuccess) return fail(cuda_error(e_, what));  \
     } while (0)
-    segs.push_back(Segment{0, 0, 1, nullptr, nullptr, 0.0f});  // the work counter, filled below
+    segs.push_back(Segment{0, 0, 4, nullptr, nullptr, 0.0f});  // the work counters, filled below
     for (int i = 0; i < n; i++) {
         const fg_batch_image &im = imgs[i];
         if (!im.params || !im.derived || !im.d_lambda || !im.d_out || !im.offsets)
@@ -243,7 +285,7 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
             const double per_block = cell_area * cell_area + 1.5 * pl.bsize * pl.bsize * p.zoom * p.zoom * p.n_samples;
             for (int by = 0; by < pl.nby; by++)
                 for (int bx = 0; bx < pl.nbx; bx++)
-                    work.push_back(CostItem{per_block, BatchItem{i, pl.bx0 + bx, pl.by0 + by, 0}});
+                    px_work.push_back(CostItem{per_block, BatchItem{i, pl.bx0 + bx, pl.by0 + by, 0}});
         } else {
             const size_t tab_bytes = grain_table_bytes(p.n_samples);
             std::vector<unsigned char> tab(tab_bytes);
@@ -281,13 +323,20 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
         }
     }
     if (smem > 200 * 1024) return fail(set_error(FG_ERR_UNSUPPORTED, "batch tile needs too much shared memory"));
-    std::stable_sort(work.begin(), work.end(), [](const CostItem &x, const CostItem &y) { return x.cost > y.cost; });
-    std::vector<BatchItem> items(work.size());
+    auto by_cost = [](const CostItem &x, const CostItem &y) { return x.cost > y.cost; };
+    std::stable_sort(work.begin(), work.end(), by_cost);
+    std::stable_sort(px_work.begin(), px_work.end(), by_cost);
+    std::vector<BatchItem> items(work.size()), px_items(px_work.size());
     for (size_t k = 0; k < work.size(); k++) items[k] = work[k].it;
+    for (size_t k = 0; k < px_work.size(); k++) px_items[k] = px_work[k].it;
     b->n_items = (int)items.size();
+    b->n_px_items = (int)px_items.size();
+    FG_BCUDA(dev_copy(b, px_items, &b->d_px_items), "batch upload");
+    FG_BCUDA(dev_alloc(b, sizeof(BatchItem) * std::max<size_t>(1, px_items.size()), (void **)&b->d_deferred),
+             "batch alloc");
     FG_BCUDA(dev_alloc(b, sizeof(int) * 4, (void **)&b->d_counter), "batch alloc");
     segs[0].a = b->d_counter;
-    add_chunks(pre, 0, 1);
+    add_chunks(pre, 0, 4);
     FG_BCUDA(dev_copy(b, images, &b->d_images), "batch upload");
     FG_BCUDA(dev_copy(b, items, &b->d_items), "batch upload");
     FG_BCUDA(dev_copy(b, segs, &b->d_segs), "batch upload");
@@ -299,8 +348,12 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
     int dev = 0, sms = 0;
     FG_BCUDA(cudaGetDevice(&dev), "device");
     FG_BCUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
-    b->grid = std::max(1, std::min(b->n_items, sms * std::max(1, tun.ctas_per_sm)));
+    b->grid = std::max(1, std::min(b->n_items + b->n_px_items, sms * std::max(1, tun.ctas_per_sm)));
+    b->lean_smem = sizeof(PwShared<PwLean>);
+    b->lean_grid = std::max(1, std::min(b->n_px_items, sms * PwLean::kCtasPerSm));
     FG_BCUDA(cudaFuncSetAttribute(batch_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+             "smem attribute");
+    FG_BCUDA(cudaFuncSetAttribute(batch_lean_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->lean_smem),
              "smem attribute");
     // capture the three launches
     cudaStream_t cs;
@@ -308,7 +361,12 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         batch_segments_kernel<<<b->n_pre_chunks, 256, 0, cs>>>(b->d_segs, b->d_pre_chunks);
-        batch_persistent_kernel<<<b->grid, 512, smem, cs>>>(b->d_images, b->d_items, b->n_items, b->d_counter);
+        if (b->n_px_items > 0)
+            batch_lean_kernel<<<b->lean_grid, PwLean::kThreads, b->lean_smem, cs>>>(b->d_images, b->d_px_items,
+                                                                                 b->n_px_items, b->d_counter,
+                                                                                 b->d_deferred);
+        batch_persistent_kernel<<<b->grid, 512, smem, cs>>>(b->d_images, b->d_items, b->n_items, b->d_counter,
+                                                            b->d_deferred);
         batch_segments_kernel<<<b->n_post_chunks, 256, 0, cs>>>(b->d_segs, b->d_post_chunks);
         e = cudaStreamEndCapture(cs, &b->graph);
     }

@@ -50,7 +50,6 @@ struct PixelwiseArgs {
     int lognorm;
     float radius_mean;
     double log_mu, log_sigma;
-    int *defer;                 // lean pass: [0] count, [1..] deferred root blocks (nbx-major); else null
 };
 
 constexpr int kGwBucketCount = 256;  // bucket index over the frac(offx)-sorted offsets

@@ -62,12 +62,16 @@ cudaError_t launch_cell_params(const float *lam, int in_w, int in_h, float delta
 
 size_t pixelwise_smem_bytes() { return sizeof(PwShared<PwFat>); }
 
-// One CTA per root block (block-grid row-major from (bx0, by0)).
+// One CTA per root block (block-grid row-major from (bx0, by0)).  With a list (lean pass), the blocks
+// left to fat CTAs are appended to it: list[0] = count, list[1..] = block indices.
 template <class C>
-__global__ void __launch_bounds__(C::kThreads, C::kCtasPerSm) pixelwise_kernel(const __grid_constant__ PixelwiseArgs a) {
+__global__ void __launch_bounds__(C::kThreads, C::kCtasPerSm)
+    pixelwise_kernel(const __grid_constant__ PixelwiseArgs a, int *__restrict__ list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    pixelwise_block<C>(a, a.bx0 + (int)(blockIdx.x % (unsigned)a.nbx), a.by0 + (int)(blockIdx.x / (unsigned)a.nbx),
-                       smem_raw);
+    const int id = (int)blockIdx.x;
+    const bool deferred = pixelwise_block<C>(a, a.bx0 + (int)(blockIdx.x % (unsigned)a.nbx),
+                                             a.by0 + (int)(blockIdx.x / (unsigned)a.nbx), smem_raw, list != nullptr);
+    if (deferred && threadIdx.x == 0) list[1 + atomicAdd(list, 1)] = id;
 }
 
 // The root blocks the lean pass deferred, in fat CTAs: persistent, each CTA taking the next listed
@@ -104,24 +108,20 @@ cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, cudaSt
     const long long nblocks = (long long)a.nbx * nby;
     if (nblocks <= 0) return cudaSuccess;
     if (!defer) {
-        pixelwise_kernel<PwFat><<<(unsigned)nblocks, PwFat::kThreads, fat_smem, s>>>(a);
+        pixelwise_kernel<PwFat><<<(unsigned)nblocks, PwFat::kThreads, fat_smem, s>>>(a, nullptr);
         return cudaGetLastError();
     }
     e = cudaMemsetAsync(defer, 0, 2 * sizeof(int), s);  // [0] the fat pass's counter, [1] the list's count
     if (e != cudaSuccess) return e;
-    PixelwiseArgs lean = a;
-    lean.defer = defer + 1;
-    pixelwise_kernel<PwLean><<<(unsigned)nblocks, PwLean::kThreads, lean_smem, s>>>(lean);
+    pixelwise_kernel<PwLean><<<(unsigned)nblocks, PwLean::kThreads, lean_smem, s>>>(a, defer + 1);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0;
     e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    PixelwiseArgs fat = a;
-    fat.defer = nullptr;
     const long long grid = std::min<long long>(nblocks, (long long)std::max(1, sms) * PwFat::kCtasPerSm);
-    pixelwise_deferred_kernel<<<(unsigned)grid, PwFat::kThreads, fat_smem, s>>>(fat, defer + 1);
+    pixelwise_deferred_kernel<<<(unsigned)grid, PwFat::kThreads, fat_smem, s>>>(a, defer + 1);
     return cudaGetLastError();
 }
 

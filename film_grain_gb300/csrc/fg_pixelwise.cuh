@@ -153,21 +153,18 @@ struct PwShared {
     float est_grains, est_cells;          // lean pass: expected grains / non-empty cells of the window
 };
 
-// Lean pass: hand the root block to the fat pass (thread 0).
-__device__ __forceinline__ void pw_defer(const PixelwiseArgs &a, int root_x, int root_y) {
-    const int slot = atomicAdd(a.defer, 1);
-    a.defer[1 + slot] = (root_y - a.by0) * a.nbx + (root_x - a.bx0);
-}
+
 
 // One root block of the pixel-wise tile kernel (all threads of the CTA; `smem_raw` holds PwShared<C>).
-// With C::kDefers and a.defer set, a root block whose window is expected to overflow the lean buffers
-// (or does overflow them) is appended to a.defer instead of being split, and produces no output here.
+// With C::kDefers and may_defer, a root block whose window is expected to overflow the lean buffers
+// (or does overflow them) is left to a fat CTA: the call produces no output and returns true.
 template <class C>
-__device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root_x, int root_y,
-                                                unsigned char *smem_raw) {
+__device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root_x, int root_y,
+                                                unsigned char *smem_raw, bool may_defer = false) {
     PwShared<C> &S = *reinterpret_cast<PwShared<C> *>(smem_raw);
     const int tid = threadIdx.x, nthreads = blockDim.x;
-    const bool lean = C::kDefers && a.defer != nullptr;
+    const bool lean = C::kDefers && may_defer;
+    bool deferred = false;
     const UniformF32 U = uniform_f32_new(0.0f, a.delta);
 
     if (tid == 0) {
@@ -223,8 +220,8 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
             }
             __syncthreads();
             if (S.est_grains > 0.75f * (float)C::kGrainMax || S.est_cells > 0.75f * (float)C::kListMax) {
-                if (tid == 0) pw_defer(a, root_x, root_y);
-                continue;  // loop head syncs
+                deferred = true;
+                continue;  // loop head syncs; the stack is empty
             }
         }
 
@@ -382,9 +379,9 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
             }
             __syncthreads();
             if (S.flags & 1) {
-                if (lean && level == 0) {  // the fat pass takes this block whole
-                    if (tid == 0) pw_defer(a, root_x, root_y);
-                    continue;  // loop head syncs
+                if (lean && level == 0) {  // a fat CTA takes this block whole
+                    deferred = true;
+                    continue;  // loop head syncs; the stack is empty
                 }
                 if (level < kPwMaxLevel) {
                     if (tid == 0) {
@@ -517,6 +514,7 @@ __device__ __forceinline__ void pixelwise_block(const PixelwiseArgs &a, int root
         }
         if (tid == 0) atomicAdd(&a.diag[3], 1ull);
     }
+    return deferred;
 }
 
 
