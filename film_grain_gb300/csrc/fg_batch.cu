@@ -41,7 +41,8 @@ struct BatchImage {
 };
 
 struct BatchItem {
-    int image, x, y, pad;
+    int image, x, y;
+    int pad;  // grain-wise: part | parts << 16
 };
 
 // One contiguous range of a segmented elementwise pass.
@@ -154,8 +155,8 @@ __global__ void __launch_bounds__(512, 2) batch_persistent_kernel(const BatchIma
         __syncthreads();
         if (threadIdx.x == 0) s_image = w.image;
         if (s_img.algo == FG_ALGO_PIXEL) pixelwise_block<PwFat>(s_img.pa, w.x, w.y, smem_raw);
-        else if (s_img.small) grainwise_tile<true>(s_img.ga, w.x, w.y, smem_raw);
-        else grainwise_tile<false>(s_img.ga, w.x, w.y, smem_raw);
+        else if (s_img.small) grainwise_tile<true>(s_img.ga, w.x, w.y, smem_raw, w.pad & 0xFFFF, w.pad >> 16);
+        else grainwise_tile<false>(s_img.ga, w.x, w.y, smem_raw, w.pad & 0xFFFF, w.pad >> 16);
         __syncthreads();
     }
 }
@@ -236,6 +237,12 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
         BatchItem it;
     };
     std::vector<CostItem> work, px_work;
+    struct GrainTile {
+        double cost;
+        BatchItem it;
+        int batches;  // the most CTAs the tile can be split over (its 32-pixel batches)
+    };
+    std::vector<GrainTile> grain_tiles;
     std::vector<Segment> segs;
     std::vector<Chunk> pre, post;
     size_t smem = pixelwise_smem_bytes();
@@ -317,12 +324,32 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
                         lam_sum = 50.0 * (x1 - x0) * (y1 - y0);
                     }
                     const double cost = lam_sum * (60.0 + 0.3 * p.n_samples) + 20.0 * (x1 - x0) * (y1 - y0);
-                    work.push_back(CostItem{cost, BatchItem{i, tx, ty, 0}});
+                    const int batches = grainwise_variant(a.n) == 0 ? 1 : ((x1 - x0) * (y1 - y0) + 31) / 32;
+                    grain_tiles.push_back(GrainTile{cost, BatchItem{i, tx, ty, 0}, batches});
                 }
             }
         }
     }
     if (smem > 200 * 1024) return fail(set_error(FG_ERR_UNSUPPORTED, "batch tile needs too much shared memory"));
+    // Heavy grain-wise tiles are split over CTAs (part | parts << 16 in the item's last word) so that no
+    // item is far above the average share of an SM slot: a tile of cost c gets ceil(c / target) parts.
+    {
+        double total_cost = 0.0;
+        for (const GrainTile &g : grain_tiles) total_cost += g.cost;
+        for (const CostItem &c : px_work) total_cost += c.cost;
+        int dev = 0, sms = 0;
+        FG_BCUDA(cudaGetDevice(&dev), "device");
+        FG_BCUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+        const double target = total_cost / (8.0 * std::max(1, sms) * std::max(1, tun.ctas_per_sm)) + 1.0;
+        for (const GrainTile &g : grain_tiles) {
+            const int parts = (int)std::max(1.0, std::min((double)std::min(g.batches, 0xFFFF), std::ceil(g.cost / target)));
+            for (int q = 0; q < parts; q++) {
+                BatchItem it = g.it;
+                it.pad = q | (parts << 16);
+                work.push_back(CostItem{g.cost / parts, it});
+            }
+        }
+    }
     auto by_cost = [](const CostItem &x, const CostItem &y) { return x.cost > y.cost; };
     std::stable_sort(work.begin(), work.end(), by_cost);
     std::stable_sort(px_work.begin(), px_work.end(), by_cost);

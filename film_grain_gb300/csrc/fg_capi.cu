@@ -210,6 +210,7 @@ GrainwiseArgs grainwise_args(const fg_params &p, const fg_derived &d, const floa
     a.rmax_h = std::max(1, std::min(a.out_h, (int)std::ceil(a.tin_h * (double)p.zoom)));
     a.rm = d.rm;
     a.zoom = p.zoom;
+    a.parts = 1;
     a.offx_min = ext[0]; a.offx_max = ext[1]; a.offy_min = ext[2]; a.offy_max = ext[3];
     // Rounding margin of the candidate intervals: each of the three f32 roundings between
     // czx + offx and the bounds() comparison moves a value by at most half an ulp of the largest
@@ -238,6 +239,10 @@ fg_status enqueue_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
     DevBuf work;  // the tile scheduler's area, freed in stream order after the launch
     FG_CUDA(work.alloc(grainwise_work_ints(a) * sizeof(int), s), "alloc tile scheduler");
     b.work = static_cast<int *>(work.p);
+    int dev = 0, sms = 0;
+    FG_CUDA(cudaGetDevice(&dev), "device");
+    FG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    b.parts = grainwise_parts(a, sms);
     FG_CUDA(launch_grainwise(b, s), "grainwise kernel");
     return FG_OK;
 }

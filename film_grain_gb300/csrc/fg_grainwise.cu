@@ -37,7 +37,7 @@ namespace fg {
 template <bool kSmall, int kVariant>
 __global__ void __launch_bounds__(kGwThreads, 2) grainwise_kernel(const __grid_constant__ GrainwiseArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    grainwise_tile<kSmall, kVariant>(a, blockIdx.x, blockIdx.y, smem_raw);
+    grainwise_tile<kSmall, kVariant>(a, blockIdx.x, blockIdx.y, smem_raw, blockIdx.z, a.parts);
 }
 
 // Persistent form: CTAs pull tiles from the scheduler's list (a.work[2..], heaviest first) through the
@@ -47,15 +47,17 @@ __global__ void __launch_bounds__(kGwThreads, 2) grainwise_persistent_kernel(con
                                                                              int ntx, int ntiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_tile;
+    const int parts = a.parts;
     for (;;) {
         if (threadIdx.x == 0) {
-            const int i = atomicAdd(a.work, 1);
-            s_tile = i < ntiles ? a.work[2 + i] : -1;
+            const int i = atomicAdd(a.work, 1);  // item i: part i % parts of the (i / parts)-th tile
+            s_tile = i < ntiles * parts ? i : -1;
         }
         __syncthreads();
-        const int t = s_tile;
-        if (t < 0) break;
-        grainwise_tile<kSmall, kVariant>(a, t % ntx, t / ntx, smem_raw);
+        const int i = s_tile;
+        if (i < 0) break;
+        const int t = a.work[2 + i / parts];
+        grainwise_tile<kSmall, kVariant>(a, t % ntx, t / ntx, smem_raw, i % parts, parts);
         __syncthreads();
     }
 }
@@ -158,6 +160,16 @@ __global__ void grainwise_epilogue_kernel(const GrainwiseEpilogueArgs a) {
 size_t grainwise_smem_bytes(const GrainwiseArgs &a) { return grainwise_tile_smem_bytes(a); }
 
 // The directed-rounding floor/ceil needs every bounds() argument within +-2^22.
+// CTAs per tile for a stand-alone launch: enough work items to give every SM about eight, never more
+// than the tile's 32-pixel batches (bitmask variants only).
+int grainwise_parts(const GrainwiseArgs &a, int sms) {
+    if (grainwise_variant(a.n) == 0) return 1;
+    const int ntiles = grainwise_tile_count(a);
+    const int batches = (a.tin_w * a.tin_h + 31) / 32;
+    const int want = (8 * sms + ntiles - 1) / std::max(1, ntiles);
+    return std::max(1, std::min(batches, want));
+}
+
 bool grainwise_small_coords(const GrainwiseArgs &a) {
     const float span = (float)max(a.out_w, a.out_h) +
                        fmaxf(fmaxf(-a.offx_min, a.offx_max), fmaxf(-a.offy_min, a.offy_max)) + a.rm * a.zoom + 4.0f;
@@ -183,7 +195,7 @@ cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
         else k = v == 4 ? grainwise_kernel<false, 4> : (v == 8 ? grainwise_kernel<false, 8> : grainwise_kernel<false, 0>);
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k<<<dim3(ntx, nty), kGwThreads, smem, s>>>(a);
+        k<<<dim3(ntx, nty, std::max(1, a.parts)), kGwThreads, smem, s>>>(a);
         return cudaGetLastError();
     }
     // tile scheduler: costs from lambda, heaviest first, persistent CTAs
@@ -207,7 +219,7 @@ cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kGwThreads, smem);
     if (e != cudaSuccess) return e;
-    const int grid = std::max(1, std::min(ntiles, sms * std::max(1, per_sm)));
+    const int grid = std::max(1, std::min(ntiles * std::max(1, a.parts), sms * std::max(1, per_sm)));
     k<<<grid, kGwThreads, smem, s>>>(a, ntx, ntiles);
     return cudaGetLastError();
 }

@@ -214,9 +214,11 @@ __device__ __forceinline__ void gb_axis_mask(const unsigned *tab, int W, float c
     }
 }
 
+// Part `part` of `parts` of a tile: a contiguous range of its 32-pixel batches (a heavy tile is split
+// over several CTAs, each with its own copy of the tile's masks; OR makes the result the same).
 template <bool kSmall, int MW>
 __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int tile_x, int tile_y,
-                                                    unsigned char *smem_raw) {
+                                                    unsigned char *smem_raw, int part, int parts) {
     const int W = (a.n + 31) >> 5;
     float2 *offk = reinterpret_cast<float2 *>(smem_raw);                         // [n] (offx, offy) by k
     unsigned *tabx = reinterpret_cast<unsigned *>(offk + ((a.n + 1) & ~1));     // [levels][buckets][W]
@@ -252,7 +254,11 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
         bk[k] =(unsigned short)((int)FG_FMUL(fx, (float)kGbBuckets) | ((int)FG_FMUL(e.x, (float)kGbBuckets) << 8));
     }
     for (int t = tid; t < region_words; t += kGwThreads) mask[t] = 0u;
-    if (tid == 0) *next_px = 0;
+    const int fw = ix1 - ix0, total = fw * (iy1 - iy0);
+    const int nbatch = (total + 31) >> 5;
+    const int px_begin = 32 * (int)(((long long)nbatch * part) / parts);
+    const int px_end = min(total, 32 * (int)(((long long)nbatch * (part + 1)) / parts));
+    if (tid == 0) *next_px = px_begin;
     __syncthreads();
     for (int t = tid; t < 2 * kGbBuckets * W; t += kGwThreads) {  // level 0: one bucket each
         const int axis = t / (kGbBuckets * W), r = t - axis * kGbBuckets * W;
@@ -277,21 +283,20 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
         __syncthreads();
     }
 
-    const int fw = ix1 - ix0, total = fw * (iy1 - iy0);
     const UniformF32 U = uniform_f32_new(0.0f, 1.0f);
     const float zoom = a.zoom;
     for (;;) {
-        // the next 32 footprint pixels of the tile (a shared counter balances the warps), one per
+        // the next 32 footprint pixels of this part (a shared counter balances the warps), one per
         // lane, Poisson set-up in step across the warp
         int base = 0;
         if (lane == 0) base = atomicAdd(next_px, 32);
         base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= total) break;
+        if (base >= px_end) break;
         const int pi = base + lane;
         uint32_t left = 0;
         int px = 0, py = 0;
         Xoshiro rng = {0, 0, 0, 0};
-        if (pi < total) {
+        if (pi < px_end) {
             px = ix0 + pi % fw;
             py = iy0 + pi / fw;
             const float lv = a.lam[(long long)py * a.in_w + px];
@@ -415,12 +420,13 @@ __device__ __forceinline__ void grainwise_tile_flat(const GrainwiseArgs &a, int 
 
 // One input tile of the grain-wise kernel (all threads of the CTA; `smem_raw` holds its shared memory).
 // kVariant: grainwise_variant(a.n), or -1 to dispatch at run time (the batched kernel).
+// parts > 1 splits the tile's pixels over CTAs (bitmask variants only; the flat variant takes whole tiles).
 template <bool kSmall, int kVariant = -1>
 __device__ __forceinline__ void grainwise_tile(const GrainwiseArgs &a, int tile_x, int tile_y,
-                                               unsigned char *smem_raw) {
+                                               unsigned char *smem_raw, int part = 0, int parts = 1) {
     const int v = kVariant >= 0 ? kVariant : grainwise_variant(a.n);
-    if (v == 4) grainwise_tile_bits<kSmall, 4>(a, tile_x, tile_y, smem_raw);
-    else if (v == 8) grainwise_tile_bits<kSmall, kGbMaxWords>(a, tile_x, tile_y, smem_raw);
+    if (v == 4) grainwise_tile_bits<kSmall, 4>(a, tile_x, tile_y, smem_raw, part, parts);
+    else if (v == 8) grainwise_tile_bits<kSmall, kGbMaxWords>(a, tile_x, tile_y, smem_raw, part, parts);
     else grainwise_tile_flat<kSmall>(a, tile_x, tile_y, smem_raw);
 }
 

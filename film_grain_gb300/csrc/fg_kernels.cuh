@@ -71,6 +71,7 @@ struct GrainwiseArgs {
     float radius_mean;
     double log_mu, log_sigma;
     int *work;                  // null: one CTA per tile; else the tile scheduler's area (grainwise_work_ints)
+    int parts;                  // CTAs per tile (>= 1; above 1 only for the bitmask variants)
 };
 
 // popcount / colour epilogue of the grain-wise path.
@@ -104,6 +105,7 @@ cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s);
 size_t grainwise_smem_bytes(const GrainwiseArgs &a);
 int grainwise_tile_count(const GrainwiseArgs &a);
 size_t grainwise_work_ints(const GrainwiseArgs &a);  // scheduler area: counter, pad, order[tiles], cost[tiles]
+int grainwise_parts(const GrainwiseArgs &a, int sms);
 cudaError_t launch_grainwise_epilogue(const GrainwiseEpilogueArgs &a, cudaStream_t s);
 cudaError_t launch_epilogue(const EpilogueArgs &a, cudaStream_t s);
 cudaError_t launch_rgb_pack(const float *p0, const float *p1, const float *p2, int n, unsigned char *out,
