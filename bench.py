@@ -487,7 +487,7 @@ def run_batch(args, rank, world):
             "e2e": {"value": samples / (t_e2e / 1e3), "unit": "samples/s", "ms_per_step": t_e2e,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "pinned lambda planes -> fg_batch_run -> pinned f32 planes"},
-            "gpu_launches": 3 * args.steps, "clocks": clk}
+            "gpu_launches": b.kernel_count * args.steps, "clocks": clk}
     if rank == 0:
         print(json.dumps(line), flush=True)
     b.close()

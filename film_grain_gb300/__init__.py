@@ -183,6 +183,7 @@ SIGNATURES = {
     "fg_batch_run": (ctypes.c_int, [ctypes.c_void_p, _vp]),
     "fg_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "fg_batch_get_tuning": (ctypes.c_int, [ctypes.c_void_p, _P(BatchTuning)]),
+    "fg_batch_kernel_count": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_int32)]),
     "fg_batch_autotune": (ctypes.c_int, [_P(_BatchImageC), ctypes.c_int32, _vp, _P(BatchTuning),
                                          _P(ctypes.c_float)]),
     "fg_sg_conv_forward": (ctypes.c_int, [ctypes.c_int32, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
@@ -422,7 +423,8 @@ def render_grainwise(lam, params: Params, derived: Derived, cancel: Optional[Cal
 
 
 def pixelwise_diagnostics() -> Tuple[int, int, int, int]:
-    """(slow-path samples, unstaged blocks, subdivisions, blocks) of this thread's last pixel-wise render."""
+    """(samples evaluated by per-sample regeneration, unstaged blocks, subdivisions, blocks) of this
+    thread's last pixel-wise render."""
     arr = (ctypes.c_ulonglong * 4)()
     lib().fg_pixelwise_diagnostics(arr)
     return tuple(int(v) for v in arr)
@@ -500,6 +502,13 @@ class Batch:
         t = BatchTuning()
         _raise(lib().fg_batch_get_tuning(self._h, ctypes.byref(t)))
         return t
+
+    @property
+    def kernel_count(self) -> int:
+        """Kernel launches one run() makes (the kernel nodes of the captured graph)."""
+        n = ctypes.c_int32()
+        _raise(lib().fg_batch_kernel_count(self._h, ctypes.byref(n)))
+        return n.value
 
     def close(self):
         if self._h:

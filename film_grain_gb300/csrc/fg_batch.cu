@@ -4,16 +4,18 @@
 // per-image entry points render them).  Creating a batch plans every image (launch plans as in
 // fg_capi.cu, under the batch's tuning), cuts the work into items -- pixel-wise root blocks and
 // grain-wise input tiles -- and sorts them by estimated cost, largest first; it then captures one
-// CUDA graph of four kernels:
+// CUDA graph of five kernels:
 //   1. a segmented kernel that zeroes the accumulators (pixel-wise output planes, grain-wise sample
 //      masks, the work counter) and builds the pixel-wise images' cell tables;
-//   2. a lean persistent kernel (256 threads, 4 CTAs per SM) over the pixel-wise root blocks, which
-//      leaves blocks too dense for its shared-memory buffers to the next kernel (as the per-image
-//      lean pass does);
-//   3. the persistent kernel: 2 CTAs per SM pull the deferred pixel-wise blocks, then the grain-wise
+//   2. the per-sample kernel over the pixel-wise images whose planes take that path per image
+//      (pixelwise_prefers_regen), one thread per output pixel;
+//   3. a lean persistent kernel (256 threads, 4 CTAs per SM) over the other pixel-wise images' root
+//      blocks, which leaves blocks too dense for its shared-memory buffers to the next kernel (as the
+//      per-image lean pass does);
+//   4. the persistent kernel: 2 CTAs per SM pull the deferred pixel-wise blocks, then the grain-wise
 //      tiles, from an atomic counter and run the same tile code as the per-image kernels
 //      (fg_pixelwise.cuh / fg_grainwise.cuh), so results are identical;
-//   4. a segmented epilogue kernel: pixel-wise count * (1/N), grain-wise popcount * (1/N).
+//   5. a segmented epilogue kernel: pixel-wise count * (1/N), grain-wise popcount * (1/N).
 // fg_batch_run replays the graph.  fg_batch_autotune times candidate tunings (grain-wise tile mask
 // budget, pixel-wise block edge, CTAs per SM) on the batch itself and returns the fastest.
 #include <algorithm>
@@ -102,6 +104,40 @@ __global__ void batch_segments_kernel(const Segment *__restrict__ segs, const Ch
 
 // counters: [0] the lean kernel's next item, [1] the persistent kernel's next item, [2] deferred items.
 
+// One image of the per-sample kernel: its CTAs are [first, first + row_ctas * out_h).
+struct RegenRange {
+    int image, row_ctas;
+    long long first;
+};
+
+// Pixel-wise images on the per-sample path (pixelwise_prefers_regen): CTA b finds its image by a
+// binary search over the ranges (ascending first) and covers 256 pixels of one of its rows.
+__global__ void __launch_bounds__(kPwRegenThreads)
+    batch_regen_kernel(const BatchImage *__restrict__ images, const RegenRange *__restrict__ ranges, int n_ranges) {
+    __shared__ int s_r;
+    __shared__ __align__(16) PixelwiseArgs s_pa;
+    const long long b = blockIdx.x;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = n_ranges - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (ranges[mid].first <= b) lo = mid;
+            else hi = mid - 1;
+        }
+        s_r = lo;
+    }
+    __syncthreads();
+    const RegenRange R = ranges[s_r];
+    {
+        const int *src = reinterpret_cast<const int *>(&images[R.image].pa);
+        int *dst = reinterpret_cast<int *>(&s_pa);
+        for (int k = threadIdx.x; k < (int)(sizeof(PixelwiseArgs) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+    }
+    __syncthreads();
+    const long long local = b - R.first;
+    pixelwise_regen_pixels(s_pa, (int)(local % R.row_ctas) * kPwRegenThreads, (int)(local / R.row_ctas));
+}
+
 // Pixel-wise items in lean CTAs (256 threads, 4 per SM); the root blocks they leave to fat CTAs are
 // appended to `deferred` for the persistent kernel.
 __global__ void __launch_bounds__(PwLean::kThreads, PwLean::kCtasPerSm)
@@ -175,6 +211,9 @@ struct fg_batch {
     BatchItem *d_px_items = nullptr;  // pixel-wise root blocks, heaviest first (the lean kernel's list)
     int n_px_items = 0;
     BatchItem *d_deferred = nullptr;  // pixel-wise blocks the lean kernel leaves to fat CTAs
+    RegenRange *d_regen = nullptr;    // pixel-wise images on the per-sample kernel
+    int n_regen = 0;
+    long long regen_ctas = 0;
     int *d_counter = nullptr;         // [0] lean next, [1] persistent next, [2] deferred count
     int lean_grid = 0;
     size_t lean_smem = 0;
@@ -243,6 +282,8 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
         int batches;  // the most CTAs the tile can be split over (its 32-pixel batches)
     };
     std::vector<GrainTile> grain_tiles;
+    std::vector<RegenRange> regen;
+    long long regen_ctas = 0;
     std::vector<Segment> segs;
     std::vector<Chunk> pre, post;
     size_t smem = pixelwise_smem_bytes();
@@ -287,9 +328,18 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
             add_chunks(pre, (int)segs.size() - 1, n_in);
             segs.push_back(Segment{2, 0, n_out, im.d_out, nullptr, 1.0f / (float)p.n_samples});
             add_chunks(post, (int)segs.size() - 1, n_out);
-            // cost: the window cells each block hashes plus its samples
+            if (pixelwise_prefers_regen(a)) {  // the per-sample kernel takes the whole image
+                const int row_ctas = (int)((d.output_width + kPwRegenThreads - 1) / kPwRegenThreads);
+                regen.push_back(RegenRange{i, row_ctas, regen_ctas});
+                regen_ctas += (long long)row_ctas * d.output_height;
+                continue;
+            }
+            // cost: the cells each block hashes (its window, or its samples' reach when that is smaller
+            // and the block regenerates) plus its samples
             const double cell_area = (double)(pl.bsize + 2.0 * d.rm) / d.delta + 4.0;
-            const double per_block = cell_area * cell_area + 1.5 * pl.bsize * pl.bsize * p.zoom * p.zoom * p.n_samples;
+            const double block_samples = (double)pl.bsize * pl.bsize * p.zoom * p.zoom * p.n_samples;
+            const double per_block =
+                std::min(cell_area * cell_area, block_samples * a.regen_cells) + 1.5 * block_samples;
             for (int by = 0; by < pl.nby; by++)
                 for (int bx = 0; bx < pl.nbx; bx++)
                     px_work.push_back(CostItem{per_block, BatchItem{i, pl.bx0 + bx, pl.by0 + by, 0}});
@@ -358,6 +408,10 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
     for (size_t k = 0; k < px_work.size(); k++) px_items[k] = px_work[k].it;
     b->n_items = (int)items.size();
     b->n_px_items = (int)px_items.size();
+    if (regen_ctas > 0x7FFFFFFFll) return fail(set_error(FG_ERR_UNSUPPORTED, "batch: too many per-sample pixels"));
+    b->n_regen = (int)regen.size();
+    b->regen_ctas = regen_ctas;
+    FG_BCUDA(dev_copy(b, regen, &b->d_regen), "batch upload");
     FG_BCUDA(dev_copy(b, px_items, &b->d_px_items), "batch upload");
     FG_BCUDA(dev_alloc(b, sizeof(BatchItem) * std::max<size_t>(1, px_items.size()), (void **)&b->d_deferred),
              "batch alloc");
@@ -382,12 +436,15 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
              "smem attribute");
     FG_BCUDA(cudaFuncSetAttribute(batch_lean_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->lean_smem),
              "smem attribute");
-    // capture the three launches
+    // capture the launches
     cudaStream_t cs;
     FG_BCUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream");
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         batch_segments_kernel<<<b->n_pre_chunks, 256, 0, cs>>>(b->d_segs, b->d_pre_chunks);
+        if (b->n_regen > 0)
+            batch_regen_kernel<<<(unsigned)b->regen_ctas, kPwRegenThreads, 0, cs>>>(b->d_images, b->d_regen,
+                                                                                  b->n_regen);
         if (b->n_px_items > 0)
             batch_lean_kernel<<<b->lean_grid, PwLean::kThreads, b->lean_smem, cs>>>(b->d_images, b->d_px_items,
                                                                                  b->n_px_items, b->d_counter,
@@ -436,6 +493,15 @@ FG_API fg_status fg_batch_destroy(fg_batch *batch) {
 FG_API fg_status fg_batch_get_tuning(const fg_batch *batch, fg_batch_tuning *out) {
     if (!batch || !out) return set_error(FG_ERR_INVALID, "null batch");
     *out = batch->tuning;
+    return FG_OK;
+}
+
+FG_API fg_status fg_batch_kernel_count(const fg_batch *batch, int32_t *out) {
+    if (!batch || !batch->graph || !out) return set_error(FG_ERR_INVALID, "null batch");
+    size_t n = 0;
+    cudaError_t e = cudaGraphGetNodes(batch->graph, nullptr, &n);
+    if (e != cudaSuccess) return cuda_error(e, "graph nodes");
+    *out = (int32_t)n;
     return FG_OK;
 }
 

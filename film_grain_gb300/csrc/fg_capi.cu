@@ -103,6 +103,10 @@ PixelwiseArgs pixelwise_args(const fg_params &p, const fg_derived &d, const PwPl
     a.n = (int)p.n_samples;
     a.rm = d.rm;
     a.delta = d.delta;
+    {
+        const double t = d.rm > 0.0f ? 2.0 * (double)d.rm / (double)d.delta + 1.0 : 0.0;
+        a.regen_cells = (float)(t * t);
+    }
     a.inv_zoom = 1.0f / p.zoom;
     a.zoom = p.zoom;
     a.bsize = pl.bsize;

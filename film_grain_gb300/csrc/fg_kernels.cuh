@@ -33,16 +33,27 @@ constexpr int kPwEdgeMax = 128;    // window cells per axis
 constexpr int kPwKChunk = 256;     // offsets per sample-assignment chunk
 constexpr int kPwFootMax = 1024;   // per-block output-pixel counters
 constexpr int kPwMaxLevel = 3;     // block subdivision depth on grain overflow
+// A block regenerates per sample (no staging) when its samples' reach, in cells, is below
+// kPwRegenSparse x its window's cells, or below kPwRegenOverflow x them once the window overflows
+// with more than kPwRegenDense of its cells non-empty.
+constexpr float kPwRegenSparse = 1.0f;
+constexpr float kPwRegenOverflow = 4.0f;
+constexpr float kPwRegenDense = 0.4f;
+// The per-sample kernel replaces the block kernel for a whole plane when an interior root block's
+// samples reach fewer than kPwRegenKernel x its window's cells (and a sample's range fits 64 cells).
+constexpr int kPwRegenThreads = 256;
+constexpr float kPwRegenKernel = 1.5f;
 
 struct PixelwiseArgs {
     const float *lam;           // in_w x in_h
     const CellParam *cells;     // in_w x in_h
     const float2 *offs;         // offsets_input [n]
     float *out;                 // out_w x out_h, accumulates hit counts (pre-zeroed)
-    unsigned long long *diag;   // [4] counters: slow samples, overflow blocks, subdivisions, blocks
+    unsigned long long *diag;   // [4] counters: regenerated samples, unstaged blocks, subdivisions, blocks
     int in_w, in_h, out_w, out_h;
     int n;
     float rm, delta, inv_zoom, zoom;
+    float regen_cells;          // mean cells one sample's own loop visits: (2 rm / delta + 1)^2
     float bsize, inv_bsize;     // block edge in input pixels (power of two) and its inverse
     int bx0, by0, nbx;          // block-grid origin and width
     float offx_min, offx_max, offy_min, offy_max;
@@ -100,6 +111,9 @@ cudaError_t launch_cell_params(const float *lam, int in_w, int in_h, float delta
 // defer: null (fat CTAs over every block) or a buffer of 2 + nbx*nby ints (lean pass, then fat CTAs
 // over the deferred blocks).
 cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, cudaStream_t s);
+// Whether a plane runs on the per-sample kernel instead of the block kernel, and its launch.
+bool pixelwise_prefers_regen(const PixelwiseArgs &a);
+cudaError_t launch_pixelwise_regen(const PixelwiseArgs &a, cudaStream_t s);
 size_t pixelwise_smem_bytes();  // the fat configuration (the batched kernel's pixel-wise items)
 cudaError_t launch_grainwise(const GrainwiseArgs &a, cudaStream_t s);
 size_t grainwise_smem_bytes(const GrainwiseArgs &a);

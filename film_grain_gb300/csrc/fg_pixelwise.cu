@@ -20,6 +20,7 @@
 // samples whose cell range leaves the staged window (never expected) and leaf blocks that still
 // overflow fall back to the reference's per-sample regeneration, which is exact too.
 #include <algorithm>
+#include <cmath>
 
 #include "fg_kernels.cuh"
 #include "fg_rng.cuh"
@@ -94,12 +95,45 @@ __global__ void __launch_bounds__(PwFat::kThreads, PwFat::kCtasPerSm)
     }
 }
 
+// Per-sample kernel: one thread per output pixel (pixelwise_regen_pixels); no shared memory, no
+// barriers.  CTA b covers pixels [256 (b % row_ctas), +256) of row b / row_ctas.
+__global__ void __launch_bounds__(kPwRegenThreads) pixelwise_regen_kernel(const __grid_constant__ PixelwiseArgs a,
+                                                                          int row_ctas) {
+    pixelwise_regen_pixels(a, (int)(blockIdx.x % (unsigned)row_ctas) * kPwRegenThreads,
+                           (int)(blockIdx.x / (unsigned)row_ctas));
+}
+
+bool pixelwise_prefers_regen(const PixelwiseArgs &a) {
+    if (!(a.rm > 0.0f)) return true;  // nothing can cover a sample: the per-sample loop exits at once
+    // a sample's range must fit the 64-bit cell mask of pixelwise_pixel
+    const double axis = std::floor(2.0 * (double)a.rm / (double)a.delta) + 2.0;
+    if (!(axis * axis <= 64.0)) return false;
+    // cell indices of every sample must stay far inside int (the flattened loop's range arithmetic)
+    const double reach = (double)std::max(a.out_w, a.out_h) / a.zoom +
+                         std::max({std::fabs(a.offx_min), std::fabs(a.offx_max), std::fabs(a.offy_min),
+                                   std::fabs(a.offy_max)}) + a.rm + 2.0;
+    if (reach / a.delta > 1.0e9) return false;
+    // an interior root block: its samples' reach in cells against its staged window
+    const double samples = (double)a.bsize * a.bsize * a.zoom * a.zoom * a.n;
+    const double edge = std::floor((a.bsize + 2.0 * a.rm) / a.delta) + 1.0;
+    return samples * a.regen_cells < kPwRegenKernel * edge * edge;
+}
+
+cudaError_t launch_pixelwise_regen(const PixelwiseArgs &a, cudaStream_t s) {
+    const long long row_ctas = (a.out_w + kPwRegenThreads - 1) / kPwRegenThreads;
+    const long long grid = row_ctas * a.out_h;
+    if (grid <= 0) return cudaSuccess;
+    pixelwise_regen_kernel<<<(unsigned)grid, kPwRegenThreads, 0, s>>>(a, (int)row_ctas);
+    return cudaGetLastError();
+}
+
 template <class K>
 static cudaError_t set_smem(K k, size_t smem) {
     return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, cudaStream_t s) {
+    if (pixelwise_prefers_regen(a)) return launch_pixelwise_regen(a, s);
     const size_t lean_smem = sizeof(PwShared<PwLean>), fat_smem = sizeof(PwShared<PwFat>);
     cudaError_t e = set_smem(pixelwise_kernel<PwLean>, lean_smem);
     if (e == cudaSuccess) e = set_smem(pixelwise_kernel<PwFat>, fat_smem);

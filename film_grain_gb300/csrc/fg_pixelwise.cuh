@@ -71,36 +71,213 @@ __device__ __forceinline__ float radius_draw(const PixelwiseArgs &a, Xoshiro &rn
     return lognormal_radius_f32(a.log_mu, a.log_sigma, rng);
 }
 
-__device__ __forceinline__ const CellParam &cell_param_at(const PixelwiseArgs &a, int i, int j) {
+// Index of the lambda pixel of cell (i, j): the cell origin's pixel, clamped to the plane
+// (src/pixelwise.rs:69-72).
+__device__ __forceinline__ long long cell_pixel(const PixelwiseArgs &a, int i, int j) {
     float sx = FG_FMUL((float)i, a.delta), sy = FG_FMUL((float)j, a.delta);
     long long ix = (long long)floorf(sx), iy = (long long)floorf(sy);
     ix = ix < 0 ? 0 : (ix > a.in_w - 1 ? a.in_w - 1 : ix);
     iy = iy < 0 ? 0 : (iy > a.in_h - 1 ? a.in_h - 1 : iy);
-    return a.cells[iy * (long long)a.in_w + ix];
+    return iy * (long long)a.in_w + ix;
 }
 
-// The reference's per-sample loop (evaluate_indicator, src/pixelwise.rs:47-106), regenerating cells.
-static __device__ bool eval_regen(const PixelwiseArgs &a, const UniformF32 &U, float xg, float yg, long long i0, long long i1,
-                           long long j0, long long j1) {
-    for (long long i = i0; i <= i1; i++) {
-        for (long long j = j0; j <= j1; j++) {
-            const CellParam cp = cell_param_at(a, (int)i, (int)j);
-            Xoshiro rng;
-            uint32_t q = cell_count(a.seed, (int)i, (int)j, cp, rng);
-            if (q == 0) continue;
-            float sx = FG_FMUL((float)i, a.delta), sy = FG_FMUL((float)j, a.delta);
-            for (uint32_t g = 0; g < q; g++) {
-                float cx = FG_FADD(sx, uniform_f32_from(U, rng.next()));
-                float cy = FG_FADD(sy, uniform_f32_from(U, rng.next()));
-                float r = radius_draw(a, rng);
-                if (r > a.rm) r = a.rm;
-                if (r <= 0.0f) continue;
-                float dx = FG_FSUB(xg, cx), dy = FG_FSUB(yg, cy);
-                if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= FG_FMUL(r, r)) return true;
-            }
-        }
+// One cell of the reference's per-sample loop: does a grain of cell (i, j), whose lambda pixel has
+// Poisson set-up cp and whose column hash is colh, cover (xg, yg)?  (src/pixelwise.rs:67-103)
+__device__ __forceinline__ bool regen_cell(const PixelwiseArgs &a, const UniformF32 &U, float xg, float yg, int i,
+                                           int j, uint64_t colh, const CellParam &cp) {
+    Xoshiro rng;
+    const uint32_t q = cell_count_h(cell_row_hash(colh, j), cp.thresh, cp.exp_lambda, rng);
+    if (q == 0) return false;
+    const float sx = FG_FMUL((float)i, a.delta), sy = FG_FMUL((float)j, a.delta);
+    for (uint32_t g = 0; g < q; g++) {
+        float cx = FG_FADD(sx, uniform_f32_from(U, rng.next()));
+        float cy = FG_FADD(sy, uniform_f32_from(U, rng.next()));
+        float r = radius_draw(a, rng);
+        if (r > a.rm) r = a.rm;
+        if (r <= 0.0f) continue;
+        float dx = FG_FSUB(xg, cx), dy = FG_FSUB(yg, cy);
+        if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= FG_FMUL(r, r)) return true;
     }
     return false;
+}
+
+// The reference's per-sample loop (evaluate_indicator, src/pixelwise.rs:47-106), regenerating the
+// cells of [i0, i1] x [j0, j1].  The indicator is an OR over the cells, so the visiting order does not
+// change it: the middle cell (the sample's own when the range is 3 wide) goes first, as it is the
+// likeliest to hold a covering grain, then the others column by column.
+static __device__ bool eval_regen(const PixelwiseArgs &a, const UniformF32 &U, float xg, float yg, int i0, int i1,
+                                  int j0, int j1) {
+    const int ic = i0 + ((i1 - i0) >> 1), jc = j0 + ((j1 - j0) >> 1);
+    if (regen_cell(a, U, xg, yg, ic, jc, cell_col_hash(a.seed, ic), a.cells[cell_pixel(a, ic, jc)])) return true;
+    for (int i = i0; i <= i1; i++) {
+        const uint64_t colh = cell_col_hash(a.seed, i);
+        for (int j = j0; j <= j1; j++)
+            if ((i != ic || j != jc) && regen_cell(a, U, xg, yg, i, j, colh, a.cells[cell_pixel(a, i, j)]))
+                return true;
+    }
+    return false;
+}
+
+// Hit count of output pixel (x, y) over its N samples by the reference's per-sample loop
+// (src/pixelwise.rs:30-38 around evaluate_indicator, src/pixelwise.rs:47-106), for sparse grains.
+// The lanes of a warp
+// (neighbouring pixels) take the samples in step, and each sample runs in two phases:
+//   1. every cell of its range gets the emptiness test alone (the first uniform against the Poisson
+//      threshold, cell_count_h): the same short work on every lane, one column hash per column;
+//   2. the non-empty cells regenerate their grains, the middle cell (the sample's own when the range
+//      is 3 wide, the likeliest to cover it) first, until one covers the sample.
+// Coverage is an OR over the cells, so the order does not change it.  A range of more than 64 cells
+// (outside the plane-level choice of this path) runs the plain loop instead.
+__device__ __forceinline__ uint32_t pixelwise_pixel_split(const PixelwiseArgs &a, const UniformF32 &U, int x,
+                                                          int y) {
+    if (!(a.rm > 0.0f)) return 0u;
+    uint32_t hits = 0;
+    for (int k = 0; k < a.n; k++) {
+        const float2 o = a.offs[k];
+        const float xg = xg_of(x, a.inv_zoom, o.x), yg = xg_of(y, a.inv_zoom, o.y);
+        const int i0 = f2i_floor(FG_FDIV(FG_FSUB(xg, a.rm), a.delta));
+        const int i1 = f2i_floor(FG_FDIV(FG_FADD(xg, a.rm), a.delta));
+        const int j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
+        const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
+        if (i0 > i1 || j0 > j1) continue;  // src/pixelwise.rs:60-62
+        const int ni = i1 - i0 + 1, nj = j1 - j0 + 1;
+        if (ni * nj > 64) {
+            hits += eval_regen(a, U, xg, yg, i0, i1, j0, j1) ? 1u : 0u;
+            continue;
+        }
+        // phase 1: bit (di * nj + dj) set when cell (i0 + di, j0 + dj) holds grains
+        unsigned long long m = 0ull;
+        long long pix = -1, thresh = 0;
+        for (int di = 0; di < ni; di++) {
+            const int i = i0 + di;
+            const uint64_t colh = cell_col_hash(a.seed, i);
+            for (int dj = 0; dj < nj; dj++) {
+                const int j = j0 + dj;
+                const long long p = cell_pixel(a, i, j);
+                if (p != pix) {
+                    pix = p;
+                    thresh = a.cells[p].thresh;
+                }
+                const uint64_t h = cell_row_hash(colh, j);
+                const uint64_t s0 = fmix64(h + kPhi), s3 = fmix64(h + 4 * kPhi);
+                const long long v = (long long)((rotl64(s0 + s3, 23) + s0) >> 11);
+                if (v > thresh) m |= 1ull << (di * nj + dj);
+            }
+        }
+        // phase 2: the non-empty cells, middle first
+        const int mid = ((ni - 1) >> 1) * nj + ((nj - 1) >> 1);
+        bool hit = false;
+        if ((m >> mid) & 1ull) {
+            m &= ~(1ull << mid);
+            const int i = i0 + (ni - 1) / 2, j = j0 + (nj - 1) / 2;
+            hit = regen_cell(a, U, xg, yg, i, j, cell_col_hash(a.seed, i), a.cells[cell_pixel(a, i, j)]);
+        }
+        while (!hit && m != 0ull) {
+            const int t = __ffsll((long long)m) - 1;
+            m &= m - 1ull;
+            const int di = t / nj, i = i0 + di, j = j0 + (t - di * nj);
+            hit = regen_cell(a, U, xg, yg, i, j, cell_col_hash(a.seed, i), a.cells[cell_pixel(a, i, j)]);
+        }
+        hits += hit ? 1u : 0u;
+    }
+    return hits;
+}
+
+// The same hit count for dense grains, where most samples are covered by the first cells they
+// visit: the loop is flattened so that each iteration visits ONE cell of the current sample and a
+// lane moves on to its next sample as soon as the current one is decided.  Each sample visits its
+// middle cell first, then the rest of its range column by column.
+__device__ __forceinline__ uint32_t pixelwise_pixel_flat(const PixelwiseArgs &a, const UniformF32 &U, int x,
+                                                         int y) {
+    if (!(a.rm > 0.0f)) return 0u;
+    uint32_t hits = 0;
+    int k = 0;
+    float xg = 0.0f, yg = 0.0f;
+    int i0 = 0, j0 = 0, ni = 0, nj = 0, ic = 0, jc = 0, ri = 0, rj = 0;
+    bool active = false, first = false;
+    int col_i = 0;
+    bool have_col = false;
+    uint64_t colh = 0;
+    long long pix = -1;
+    CellParam cp;
+    cp.thresh = 0; cp.exp_lambda = 0.0;
+    while (true) {
+        if (!active) {
+            if (k >= a.n) break;
+            const float2 o = a.offs[k];
+            xg = xg_of(x, a.inv_zoom, o.x);
+            yg = xg_of(y, a.inv_zoom, o.y);
+            i0 = f2i_floor(FG_FDIV(FG_FSUB(xg, a.rm), a.delta));
+            const int i1 = f2i_floor(FG_FDIV(FG_FADD(xg, a.rm), a.delta));
+            j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
+            const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
+            if (i0 > i1 || j0 > j1) {  // src/pixelwise.rs:60-62
+                k++;
+                continue;
+            }
+            ni = i1 - i0 + 1;
+            nj = j1 - j0 + 1;
+            ic = (ni - 1) >> 1;
+            jc = (nj - 1) >> 1;
+            ri = 0; rj = 0;
+            first = true;
+            active = true;
+        }
+        const int i = i0 + (first ? ic : ri), j = j0 + (first ? jc : rj);
+        if (!have_col || i != col_i) {
+            col_i = i;
+            have_col = true;
+            colh = cell_col_hash(a.seed, i);
+        }
+        const long long p = cell_pixel(a, i, j);
+        if (p != pix) {
+            pix = p;
+            cp = a.cells[p];
+        }
+        const bool hit = regen_cell(a, U, xg, yg, i, j, colh, cp);
+        if (first) {
+            first = false;
+        } else if (++rj == nj) {
+            rj = 0;
+            ++ri;
+        }
+        if (ri == ic && rj == jc && ++rj == nj) {  // the middle cell went first: skip it
+            rj = 0;
+            ++ri;
+        }
+        if (hit || ri >= ni) {
+            hits += hit ? 1u : 0u;
+            k++;
+            active = false;
+        }
+    }
+    return hits;
+}
+
+// The per-sample path for the kPwRegenThreads pixels [x0, x0 + kPwRegenThreads) of row y (one per
+// thread of the CTA): each warp (32 neighbouring pixels) takes the dense form when most of its pixels
+// expect more than ln 2 grains per cell (over half the cells non-empty), else the sparse form, and
+// writes the hit counts.  Thread 0 adds the CTA's samples and the CTA to the diagnostics
+// (regenerated samples, unstaged blocks, blocks).
+__device__ __forceinline__ void pixelwise_regen_pixels(const PixelwiseArgs &a, int x0, int y) {
+    const int x = x0 + (int)threadIdx.x;
+    if (threadIdx.x == 0) {
+        const int px = min(kPwRegenThreads, a.out_w - x0);
+        atomicAdd(&a.diag[0], (unsigned long long)px * (unsigned long long)a.n);
+        atomicAdd(&a.diag[1], 1ull);
+        atomicAdd(&a.diag[3], 1ull);
+    }
+    bool dense = false;
+    if (x < a.out_w) {
+        const int xi = min(a.in_w - 1, max(0, (int)floorf(((float)x + 0.5f) * a.inv_zoom)));
+        const int yi = min(a.in_h - 1, max(0, (int)floorf(((float)y + 0.5f) * a.inv_zoom)));
+        dense = a.lam[(long long)yi * a.in_w + xi] * a.delta * a.delta > 0.6931472f;
+    }
+    const bool flat = __popc(__ballot_sync(0xffffffffu, dense)) >= 16;
+    if (x >= a.out_w) return;
+    const UniformF32 U = uniform_f32_new(0.0f, a.delta);
+    const uint32_t hits = flat ? pixelwise_pixel_flat(a, U, x, y) : pixelwise_pixel_split(a, U, x, y);
+    a.out[(long long)y * a.out_w + x] = (float)hits;
 }
 
 // Block-wide exclusive scan of one int per thread (any blockDim.x that is a multiple of 32, <= 1024).
@@ -185,13 +362,23 @@ __device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root
         const float X0 = FG_FMUL((float)sbx, bs), X1 = FG_FMUL((float)(sbx + 1), bs);
         const float Y0 = FG_FMUL((float)sby, bs), Y1 = FG_FMUL((float)(sby + 1), bs);
 
+        // ---- staged window of cells
+        // Every owned sample has xg in [X0, X1) and computes its cell range with these same rounded
+        // operations, which are monotone, so its range lies inside [wi0, wi1] x [wj0, wj1].
+        const int wi0 = f2i_floor(FG_FDIV(FG_FSUB(X0, a.rm), a.delta));
+        const int wi1 = f2i_floor(FG_FDIV(FG_FADD(X1, a.rm), a.delta));
+        const int wj0 = f2i_floor(FG_FDIV(FG_FSUB(Y0, a.rm), a.delta));
+        const int wj1 = f2i_floor(FG_FDIV(FG_FADD(Y1, a.rm), a.delta));
+        const long long Wc = (long long)wi1 - wi0 + 1, Hc = (long long)wj1 - wj0 + 1;
+        const bool window_fits = Wc > 0 && Hc > 0 && Wc <= kPwEdgeMax && Hc <= kPwEdgeMax && Wc * Hc <= kPwCellMax;
+        const int nc = window_fits ? (int)(Wc * Hc) : 0;
+
+        bool regen_dense = false;
         if (lean && level == 0) {
             // expected grains and non-empty cells of the window: lambda integrated over its rectangle
             // (a cell takes the lambda of the pixel containing its origin; edge pixels extend outwards)
-            const float wx0 = FG_FMUL((float)(f2i_floor(FG_FDIV(FG_FSUB(X0, a.rm), a.delta))), a.delta);
-            const float wx1 = FG_FMUL((float)(f2i_floor(FG_FDIV(FG_FADD(X1, a.rm), a.delta)) + 1), a.delta);
-            const float wy0 = FG_FMUL((float)(f2i_floor(FG_FDIV(FG_FSUB(Y0, a.rm), a.delta))), a.delta);
-            const float wy1 = FG_FMUL((float)(f2i_floor(FG_FDIV(FG_FADD(Y1, a.rm), a.delta)) + 1), a.delta);
+            const float wx0 = FG_FMUL((float)wi0, a.delta), wx1 = FG_FMUL((float)(wi1 + 1), a.delta);
+            const float wy0 = FG_FMUL((float)wj0, a.delta), wy1 = FG_FMUL((float)(wj1 + 1), a.delta);
             const int px0 = (int)floorf(wx0), px1 = (int)floorf(wx1), py0 = (int)floorf(wy0), py1 = (int)floorf(wy1);
             const int nx = px1 - px0 + 1, npx = nx * (py1 - py0 + 1);
             if (tid == 0) { S.est_grains = 0.0f; S.est_cells = 0.0f; }
@@ -220,10 +407,17 @@ __device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root
             }
             __syncthreads();
             if (S.est_grains > 0.75f * (float)C::kGrainMax || S.est_cells > 0.75f * (float)C::kListMax) {
-                deferred = true;
-                continue;  // loop head syncs; the stack is empty
+                // an interior block's samples (border blocks own fewer)
+                const float reach_est = FG_FMUL(FG_FMUL(bs, bs), a.zoom * a.zoom) * (float)a.n * a.regen_cells;
+                if (reach_est < kPwRegenOverflow * (float)nc && S.est_cells > kPwRegenDense * (float)nc) {
+                    regen_dense = true;
+                } else {
+                    deferred = true;
+                    continue;  // loop head syncs; the stack is empty
+                }
             }
         }
+
 
         // ---- ownership: rectangles per offset, sample total and pixel footprint
         if (tid == 0) { S.fx0 = 0x7fffffff; S.fx1 = -1; S.fy0 = 0x7fffffff; S.fy1 = -1; S.nsamples = 0; }
@@ -262,21 +456,19 @@ __device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root
         const int fx0 = S.fx0, fy0 = S.fy0, fw = S.fx1 - S.fx0, fh = S.fy1 - S.fy0;
         const bool use_cnt = (long long)fw * fh <= kPwFootMax;
 
-        // ---- staged window of cells
-        // Every owned sample has xg in [X0, X1) and computes its cell range with these same rounded
-        // operations, which are monotone, so its range lies inside [wi0, wi1] x [wj0, wj1].
-        const int wi0 = f2i_floor(FG_FDIV(FG_FSUB(X0, a.rm), a.delta));
-        const int wi1 = f2i_floor(FG_FDIV(FG_FADD(X1, a.rm), a.delta));
-        const int wj0 = f2i_floor(FG_FDIV(FG_FSUB(Y0, a.rm), a.delta));
-        const int wj1 = f2i_floor(FG_FDIV(FG_FADD(Y1, a.rm), a.delta));
-        const long long Wc = (long long)wi1 - wi0 + 1, Hc = (long long)wj1 - wj0 + 1;
-        const bool window_fits = Wc > 0 && Hc > 0 && Wc <= kPwEdgeMax && Hc <= kPwEdgeMax && Wc * Hc <= kPwCellMax;
-        const int nc = window_fits ? (int)(Wc * Hc) : 0;
+        // ---- staging or regeneration.  Staging visits every window cell once; regeneration (the
+        // reference's own per-sample loop) visits each owned sample's reach of ~regen_cells cells, with
+        // an early exit on the first covering grain.  Blocks whose samples reach fewer cells than the
+        // window holds (border blocks, which own few samples) regenerate, and so do dense windows that
+        // overflow shared memory: they would stage again at every subdivision level, while most of
+        // their samples are covered by the first cells they visit.
+        const float reach = (float)S.nsamples * a.regen_cells;
+        const bool regen = regen_dense || (window_fits && reach < kPwRegenSparse * (float)nc);
 
         if (use_cnt)
             for (int t = tid; t < fw * fh; t += nthreads) S.cnt[t] = 0u;
         if (tid == 0) { S.nlist = 0; S.flags = 0; }
-        if (window_fits) {
+        if (window_fits && !regen) {
             for (int t = tid; t < Wc; t += nthreads) {
                 long long ix = (long long)floorf(FG_FMUL((float)(wi0 + t), a.delta));
                 S.colix[t] = (int)(ix < 0 ? 0 : (ix > a.in_w - 1 ? a.in_w - 1 : ix));
@@ -289,7 +481,7 @@ __device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root
         __syncthreads();
 
         bool staged = false;
-        if (window_fits) {
+        if (window_fits && !regen) {
             // ---- pass A1: which window cells hold grains.  The first uniform alone decides q == 0
             // (cell_count_h), so every cell costs the same; each thread walks a contiguous run of cells
             // in column-major order, reusing the column stage of the cell hash and the lambda pixel's
@@ -379,11 +571,12 @@ __device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root
             }
             __syncthreads();
             if (S.flags & 1) {
-                if (lean && level == 0) {  // a fat CTA takes this block whole
+                if (reach < kPwRegenOverflow * (float)nc && (float)S.nlist > kPwRegenDense * (float)nc) {
+                    // regenerated in pass C (staged stays false)
+                } else if (lean && level == 0) {  // a fat CTA takes this block whole
                     deferred = true;
                     continue;  // loop head syncs; the stack is empty
-                }
-                if (level < kPwMaxLevel) {
+                } else if (level < kPwMaxLevel) {
                     if (tid == 0) {
                         atomicAdd(&a.diag[2], 1ull);
                         for (int q = 0; q < 4; q++) {

@@ -228,6 +228,8 @@ FG_API fg_status fg_batch_create(const fg_batch_image *images, int32_t n_images,
 FG_API fg_status fg_batch_run(fg_batch *batch, void *stream);
 FG_API fg_status fg_batch_destroy(fg_batch *batch);
 FG_API fg_status fg_batch_get_tuning(const fg_batch *batch, fg_batch_tuning *out);
+/* Kernel launches one fg_batch_run makes (the kernel nodes of its graph).  No counterpart in the crate. */
+FG_API fg_status fg_batch_kernel_count(const fg_batch *batch, int32_t *out);
 /* Times candidate tunings on these images (creating and running a batch for each) and returns the
  * fastest, with its graph time in milliseconds when best_ms is not NULL.  Synchronous. */
 FG_API fg_status fg_batch_autotune(const fg_batch_image *images, int32_t n_images, void *stream,

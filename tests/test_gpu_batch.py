@@ -39,6 +39,8 @@ def test_batch_matches_per_image(cuda, fgl):
     torch = cuda
     images, want = _images(fgl, torch, SPECS)
     b = fgl.Batch(images)
+    # zeroing, per-sample, lean, persistent and epilogue kernels
+    assert b.kernel_count == 5
     for _ in range(2):  # two replays of the captured graph
         b.run()
         torch.cuda.synchronize()
