@@ -186,10 +186,16 @@ constexpr int kGbMaxWords = 8;   // N <= 256
 
 __host__ __device__ inline bool grainwise_uses_bits(int n) { return n <= 32 * kGbMaxWords; }
 
+// Words between consecutive table entries: W rounded up to odd, so that the lanes of a warp reading
+// word w of the entries of different buckets b hit different banks ((b * S + w) mod 32 is one-to-one
+// in b mod 32 for odd S); with the stride W = 8 they met on 4 banks.
+__host__ __device__ inline int gb_entry_stride(int W) { return W | 1; }
+
 // The samples whose frac(offset) lies in the cyclic interval [c - h, c + h] (c in [0, 1)), rounded out
 // to whole buckets, written to m (kAnd = false) or ANDed into it (kAnd = true).
 template <int MW, bool kAnd>
-__device__ __forceinline__ void gb_axis_mask(const unsigned *tab, int W, float c, float h, int n, unsigned (&m)[MW]) {
+__device__ __forceinline__ void gb_axis_mask(const unsigned *tab, int W, int S, float c, float h, int n,
+                                             unsigned (&m)[MW]) {
     const int blo = __float2int_rd(FG_FMUL(FG_FSUB(c, h), (float)kGbBuckets));
     const int bhi = __float2int_rd(FG_FMUL(FG_FADD(c, h), (float)kGbBuckets));
     const int len = bhi - blo + 1;
@@ -205,8 +211,8 @@ __device__ __forceinline__ void gb_axis_mask(const unsigned *tab, int W, float c
     }
     const int b0 = blo & (kGbBuckets - 1);
     const int L = 31 - __clz(len);
-    const unsigned *e0 = tab + (L * kGbBuckets + b0) * W;
-    const unsigned *e1 = tab + (L * kGbBuckets + ((b0 + len - (1 << L)) & (kGbBuckets - 1))) * W;
+    const unsigned *e0 = tab + (L * kGbBuckets + b0) * S;
+    const unsigned *e1 = tab + (L * kGbBuckets + ((b0 + len - (1 << L)) & (kGbBuckets - 1))) * S;
 #pragma unroll
     for (int w = 0; w < MW; w++) {
         const unsigned v = w < W ? (e0[w] | e1[w]) : 0u;
@@ -221,9 +227,10 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
                                                     unsigned char *smem_raw, int part, int parts) {
     const int W = (a.n + 31) >> 5;
     float2 *offk = reinterpret_cast<float2 *>(smem_raw);                         // [n] (offx, offy) by k
-    unsigned *tabx = reinterpret_cast<unsigned *>(offk + ((a.n + 1) & ~1));     // [levels][buckets][W]
-    unsigned *taby = tabx + kGbLevels * kGbBuckets * W;
-    unsigned short *bk = reinterpret_cast<unsigned short *>(taby + kGbLevels * kGbBuckets * W);  // [n] buckets
+    const int S = gb_entry_stride(W);
+    unsigned *tabx = reinterpret_cast<unsigned *>(offk + ((a.n + 1) & ~1));     // [levels][buckets][S]
+    unsigned *taby = tabx + kGbLevels * kGbBuckets * S;
+    unsigned short *bk = reinterpret_cast<unsigned short *>(taby + kGbLevels * kGbBuckets * S);  // [n] buckets
     int *next_px = reinterpret_cast<int *>(bk + ((a.n + 7) & ~7));             // [4]: batch counter
     unsigned int *mask = reinterpret_cast<unsigned int *>(next_px + 4);
     const int tid = threadIdx.x, lane = tid & 31;
@@ -268,7 +275,7 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
             const int k = w * 32 + j;
             if (k < a.n && ((bk[k] >> (8 * axis)) & 0xFF) == b) bits |= 1u << j;
         }
-        (axis ? taby : tabx)[b * W + w] = bits;
+        (axis ? taby : tabx)[b * S + w] = bits;
     }
     __syncthreads();
     for (int L = 1; L < kGbLevels; L++) {
@@ -277,8 +284,8 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
             const int b = r / W, w = r - b * W;
             unsigned *tb = axis ? taby : tabx;
             const int b2 = (b + (1 << (L - 1))) & (kGbBuckets - 1);
-            tb[(L * kGbBuckets + b) * W + w] = tb[((L - 1) * kGbBuckets + b) * W + w] |
-                                               tb[((L - 1) * kGbBuckets + b2) * W + w];
+            tb[(L * kGbBuckets + b) * S + w] = tb[((L - 1) * kGbBuckets + b) * S + w] |
+                                               tb[((L - 1) * kGbBuckets + b2) * S + w];
         }
         __syncthreads();
     }
@@ -331,8 +338,8 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
                         gy = czy;
                         gr = ro;
                         const float h = FG_FADD(ro, a.frac_eps);
-                        gb_axis_mask<MW, false>(tabx, W, cxf, h, a.n, m);
-                        gb_axis_mask<MW, true>(taby, W, cyf, h, a.n, m);
+                        gb_axis_mask<MW, false>(tabx, W, S, cxf, h, a.n, m);
+                        gb_axis_mask<MW, true>(taby, W, S, cyf, h, a.n, m);
 #pragma unroll
                         for (int w = 0; w < MW; w++) cnt += __popc(m[w]);
                     }
@@ -405,7 +412,8 @@ __device__ __forceinline__ void grainwise_tile_bits(const GrainwiseArgs &a, int 
 
 inline size_t grainwise_bits_smem_bytes(const GrainwiseArgs &a) {
     const size_t W = (size_t)(a.n + 31) / 32;
-    return (size_t)((a.n + 1) & ~1) * sizeof(float2) + 2 * (size_t)kGbLevels * kGbBuckets * W * sizeof(unsigned) +
+    return (size_t)((a.n + 1) & ~1) * sizeof(float2) +
+           2 * (size_t)kGbLevels * kGbBuckets * gb_entry_stride((int)W) * sizeof(unsigned) +
            (size_t)((a.n + 7) & ~7) * sizeof(unsigned short) + 4 * sizeof(int) +
            (size_t)a.rmax_w * a.rmax_h * a.words * sizeof(unsigned int);
 }
