@@ -382,7 +382,8 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
     }
     if (smem > 200 * 1024) return fail(set_error(FG_ERR_UNSUPPORTED, "batch tile needs too much shared memory"));
     // Heavy grain-wise tiles are split over CTAs (part | parts << 16 in the item's last word) so that no
-    // item is far above the average share of an SM slot: a tile of cost c gets ceil(c / target) parts.
+    // item is far above the average share of an SM slot: a tile of cost c gets ceil(c / target) parts,
+    // at most one per kGwWarps of its 32-pixel batches.
     {
         double total_cost = 0.0;
         for (const GrainTile &g : grain_tiles) total_cost += g.cost;
@@ -392,7 +393,8 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
         FG_BCUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
         const double target = total_cost / (8.0 * std::max(1, sms) * std::max(1, tun.ctas_per_sm)) + 1.0;
         for (const GrainTile &g : grain_tiles) {
-            const int parts = (int)std::max(1.0, std::min((double)std::min(g.batches, 0xFFFF), std::ceil(g.cost / target)));
+            const int most = std::max(1, std::min(g.batches / kGwWarps, 0xFFFF));  // a batch per warp at least
+            const int parts = (int)std::max(1.0, std::min((double)most, std::ceil(g.cost / target)));
             for (int q = 0; q < parts; q++) {
                 BatchItem it = g.it;
                 it.pad = q | (parts << 16);

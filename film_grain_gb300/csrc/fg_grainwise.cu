@@ -160,14 +160,15 @@ __global__ void grainwise_epilogue_kernel(const GrainwiseEpilogueArgs a) {
 size_t grainwise_smem_bytes(const GrainwiseArgs &a) { return grainwise_tile_smem_bytes(a); }
 
 // The directed-rounding floor/ceil needs every bounds() argument within +-2^22.
-// CTAs per tile for a stand-alone launch: enough work items to give every SM about eight, never more
-// than the tile's 32-pixel batches (bitmask variants only).
+// CTAs per tile for a stand-alone launch: enough work items to give every SM about eight, never so
+// many that a part has fewer 32-pixel batches than the CTA has warps (bitmask variants only).
 int grainwise_parts(const GrainwiseArgs &a, int sms) {
     if (grainwise_variant(a.n) == 0) return 1;
     const int ntiles = grainwise_tile_count(a);
     const int batches = (a.tin_w * a.tin_h + 31) / 32;
     const int want = (8 * sms + ntiles - 1) / std::max(1, ntiles);
-    return std::max(1, std::min(batches, want));
+    // each part keeps at least one 32-pixel batch per warp: fewer leave warps idle at the tile's end
+    return std::max(1, std::min(std::max(1, batches / kGwWarps), want));
 }
 
 bool grainwise_small_coords(const GrainwiseArgs &a) {
