@@ -51,6 +51,14 @@ WORKLOADS = {
     "pixel_rgb_1024": dict(desc="profiling case: pixel-wise RGB 1024x1024x3 blobs, lognormal r 0.025/0.01, N 256",
                            w=1024, h=1024, mode="rgb", algo="pixel", radius=0.025, dist="lognorm", sd=0.01, zoom=1.0,
                            n=256, seed=42, image_seed=1),
+    "grain_luma_512_saturated": dict(desc="profiling case: grain-wise luma 512x512 saturated plane (u = 1), const r "
+                                          "0.025, N 256, zoom 1 (about 7000 grains per pixel)",
+                                     w=512, h=512, mode="luma", algo="grain", radius=0.025, dist="const", sd=0.0,
+                                     zoom=1.0, n=256, seed=42, image_seed=0, source="flat", level=1.0),
+    "pixel_luma_2048_sparse": dict(desc="profiling case: pixel-wise luma 2048x2048 blobs, const r 0.025, N 64, zoom 1 "
+                                        "(the per-sample kernel)",
+                                   w=2048, h=2048, mode="luma", algo="pixel", radius=0.025, dist="const", sd=0.0,
+                                   zoom=1.0, n=64, seed=42, image_seed=5, source="blobs"),
     "pixel_rgb_4096": dict(desc="plain pixel-wise RGB 4096x4096x3 blobs, lognormal r 0.025/0.01, N 256, zoom 1",
                            w=4096, h=4096, mode="rgb", algo="pixel", radius=0.025, dist="lognorm", sd=0.01, zoom=1.0,
                            n=256, seed=42, image_seed=1),
@@ -63,6 +71,11 @@ def log(*a):
 
 def make_input(wl):
     from film_grain_gb300 import workloads
+    source = wl.get("source")
+    if source == "flat":
+        return np.full((wl["h"], wl["w"], 3), wl["level"], np.float32)
+    if source == "blobs":
+        return workloads.gray_rgb(workloads.blobs_plane(wl["w"], wl["h"], wl["image_seed"]))
     if wl["mode"] == "luma" and wl["algo"] == "pixel":
         return workloads.gray_rgb(workloads.ramp_noise(wl["w"], wl["h"], wl["image_seed"]))
     return workloads.blobs_rgb(wl["w"], wl["h"], wl["image_seed"])
@@ -210,6 +223,29 @@ def pixelwise_lane_ops(lam, wl, derived, out_px):
     terms = dict(cells=cells, nonempty_cells=nonempty, grains=grains, samples=samples, tests=tests)
     terms["total"] = (PW_COST["cell"] * cells + PW_COST["nonempty"] * nonempty + c_g * grains +
                       PW_COST["sample"] * samples + PW_COST["test"] * tests)
+    return terms
+
+
+# The per-sample path (planes whose samples reach fewer cells than a staged window): every sample
+# decides emptiness for the cells of its range (hash + threshold) and regenerates the non-empty ones
+# until a grain covers it.  Minimal lane-ops: a sample's set-up, one emptiness test per cell of its
+# range, and a Poisson draw plus the grains' generation and disk tests for each non-empty cell; the
+# early exit is credited as half the non-empty cells of a covered sample.
+PW_REGEN_COST = dict(sample=40, cell=45, nonempty=60, grain=30)
+
+
+def pixelwise_regen_lane_ops(lam, wl, derived, out_px):
+    lam = lam.astype(np.float64)
+    d, rm = float(derived.delta), float(derived.rm)
+    cells = (2.0 * rm / d + 1.0) ** 2  # cells of one sample's range
+    samples = float(out_px) * wl["n"]
+    p_ne = float(np.mean(1.0 - np.exp(-lam * d * d)))
+    u = float(np.mean(1.0 - np.exp(-lam / float(derived.inv_e_pi_r2))))
+    nonempty = samples * cells * p_ne * (1.0 - u / 2)
+    grains = samples * cells * float(np.mean(lam * d * d)) * (1.0 - u / 2)
+    terms = dict(samples=samples, cells=samples * cells, nonempty_cells=nonempty, grains=grains)
+    terms["total"] = (PW_REGEN_COST["sample"] * samples + PW_REGEN_COST["cell"] * samples * cells +
+                      PW_REGEN_COST["nonempty"] * nonempty + PW_REGEN_COST["grain"] * grains)
     return terms
 
 
@@ -581,8 +617,9 @@ def main():
     sp = stream.cuda_stream
     offs = np.ascontiguousarray(derived.offsets if wl["algo"] == "grain" else derived.offsets_input, np.float32)
     fn = L.fg_render_grainwise_async if wl["algo"] == "grain" else L.fg_render_pixelwise_async
-    # grain: tile costs, tile order, persistent tiles, popcount; pixel: cells, tiles, epilogue
-    launches_per_plane = 4 if wl["algo"] == "grain" else 3
+    # grain: tile costs, tile order, persistent tiles, popcount; pixel: cell table, per-sample kernel or
+    # lean + fat block passes, epilogue
+    launches_per_plane = 4 if wl["algo"] == "grain" else fg.pixelwise_kernel_count(params, derived)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     ev = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in planes] for _ in range(args.steps)]
@@ -701,7 +738,15 @@ def main():
                             "kernel": "grainwise_persistent_kernel (launch_ms: the whole plane)", "launch_ms": launch_ms,
                             "lane_ops_per_launch": ops, "counts": counts,
                             "peak_basis": f"{sm_count} SMs x 128 lanes x {f_mhz:.0f} MHz (sampled)"}
-    if wl["algo"] == "pixel":
+    if wl["algo"] == "pixel" and launches_per_plane == 3:
+        ops = [pixelwise_regen_lane_ops(lh, wl, derived, ow * oh) for lh in lam_host]
+        ach = sum(o["total"] / (ms / 1e3) for o, ms in zip(ops, launch_ms)) / len(ops)
+        line["roofline"] = {"bound": "sm_issue", "achieved": ach / 1e12, "peak": peak / 1e12, "unit": "Tlane-op/s",
+                            "frac": ach / peak, "traffic": None,
+                            "kernel": "pixelwise_regen_kernel (launch_ms: the whole plane)", "launch_ms": launch_ms,
+                            "lane_ops_per_launch": [o["total"] for o in ops], "model_terms": ops[0],
+                            "peak_basis": f"{sm_count} SMs x 128 lanes x {f_mhz:.0f} MHz (sampled)"}
+    elif wl["algo"] == "pixel":
         ops = [pixelwise_lane_ops(lh, wl, derived, ow * oh) for lh in lam_host]
         ach = sum(o["total"] / (ms / 1e3) for o, ms in zip(ops, launch_ms)) / len(ops)
         line["roofline"] = {"bound": "sm_issue", "achieved": ach / 1e12, "peak": peak / 1e12, "unit": "Tlane-op/s",

@@ -30,7 +30,8 @@ __all__ = [
     "RadiusDist", "Algo", "ColorMode", "MaxRadius", "Roi", "ParamsBuilder", "Params", "Derived", "RenderStats",
     "RenderError", "ParamsError", "CancelledError", "GpuError", "derive_common", "default_cell_delta",
     "normalize_plane", "lambda_plane", "choose_algorithm", "render_pixelwise", "render_grainwise",
-    "render_with_input_image", "dry_run_with_input_image", "lib", "pixelwise_diagnostics", "make_offsets",
+    "render_with_input_image", "dry_run_with_input_image", "lib", "pixelwise_diagnostics", "pixelwise_kernel_count",
+    "make_offsets",
     "Batch", "BatchTuning",
 ]
 
@@ -179,6 +180,7 @@ SIGNATURES = {
     "fg_last_error_message": (ctypes.c_char_p, []),
     "fg_version": (ctypes.c_char_p, []),
     "fg_pixelwise_diagnostics": (None, [_P(ctypes.c_ulonglong)]),
+    "fg_pixelwise_kernel_count": (ctypes.c_int, [_P(_ParamsC), _P(_DerivedC), ctypes.c_void_p, _P(ctypes.c_int32)]),
     "fg_batch_create": (ctypes.c_int, [_P(_BatchImageC), ctypes.c_int32, _P(BatchTuning), _P(ctypes.c_void_p)]),
     "fg_batch_run": (ctypes.c_int, [ctypes.c_void_p, _vp]),
     "fg_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -420,6 +422,15 @@ def render_grainwise(lam, params: Params, derived: Derived, cancel: Optional[Cal
     """render_grainwise (src/grainwise.rs:12-124).  lam: numpy (host) or torch CUDA tensor."""
     return _render("fg_render_grainwise", lam, params, derived, cancel,
                    np.ascontiguousarray(derived.offsets, np.float32))
+
+
+def pixelwise_kernel_count(params: "Params", derived: "Derived") -> int:
+    """Kernel launches one pixel-wise render of these params makes: 3 on the per-sample kernel, 4 on the
+    block kernels."""
+    offs = np.ascontiguousarray(derived.offsets_input, np.float32)
+    n = ctypes.c_int32()
+    _raise(lib().fg_pixelwise_kernel_count(params.c, derived._c, offs.ctypes.data, ctypes.byref(n)))
+    return n.value
 
 
 def pixelwise_diagnostics() -> Tuple[int, int, int, int]:

@@ -522,4 +522,16 @@ FG_API void fg_pixelwise_diagnostics(unsigned long long out[4]) {
     for (int i = 0; i < 4; i++) out[i] = g_pw_diag[i];
 }
 
+FG_API fg_status fg_pixelwise_kernel_count(const fg_params *params, const fg_derived *derived,
+                                           const float *offsets_input, int32_t *out) {
+    if (!params || !derived || !offsets_input || !out) return set_error(FG_ERR_INVALID, "null argument");
+    fg_status st = check_render_args(params, derived);
+    if (st != FG_OK) return st;
+    const PwPlan pl = plan_pixelwise(*params, *derived, offsets_input, 4);
+    const PixelwiseArgs a = pixelwise_args(*params, *derived, pl, nullptr, nullptr, nullptr, nullptr, nullptr);
+    *out = pixelwise_prefers_regen(a) ? 3 : 4;
+    clear_error();
+    return FG_OK;
+}
+
 }  // extern "C"
