@@ -120,63 +120,119 @@ static __device__ bool eval_regen(const PixelwiseArgs &a, const UniformF32 &U, f
 
 // Hit count of output pixel (x, y) over its N samples by the reference's per-sample loop
 // (src/pixelwise.rs:30-38 around evaluate_indicator, src/pixelwise.rs:47-106), for sparse grains.
-// The lanes of a warp
-// (neighbouring pixels) take the samples in step, and each sample runs in two phases:
+// Called by all 32 lanes of a warp (neighbouring pixels; `valid` false for lanes past the row's end,
+// which take part without samples); the lanes take the samples in step, and each sample runs in two
+// phases:
 //   1. every cell of its range gets the emptiness test alone (the first uniform against the Poisson
-//      threshold, cell_count_h): the same short work on every lane, one column hash per column;
-//   2. the non-empty cells regenerate their grains, the middle cell (the sample's own when the range
-//      is 3 wide, the likeliest to cover it) first, until one covers the sample.
-// Coverage is an OR over the cells, so the order does not change it.  A range of more than 64 cells
-// (outside the plane-level choice of this path) runs the plain loop instead.
-__device__ __forceinline__ uint32_t pixelwise_pixel_split(const PixelwiseArgs &a, const UniformF32 &U, int x,
-                                                          int y) {
+//      threshold, cell_count_h): the same short work on every lane, one column hash per column; the
+//      non-empty cells go to a 64-bit mask, cell (i0 + di, j0 + dj) at bit di * 8 + dj with the middle
+//      cell swapped into bit 0;
+//   2. the (lane, non-empty cell) pairs of the whole warp are dealt out 32 at a time: pair p goes to
+//      lane p % 32, which finds its owner by a shuffle binary search over the inclusive counts and the
+//      cell by a rank-select in the owner's mask, regenerates that cell's grains against the owner's
+//      sample and ORs a hit back to the owner (pairs of owners already covered are skipped).
+// Coverage is an OR over the cells, so neither the order nor the dealing changes it.  A range wider
+// than 8 cells on an axis (outside the plane-level choice of this path) runs the plain loop instead.
+__device__ __forceinline__ uint32_t pixelwise_pixel_split(const PixelwiseArgs &a, const UniformF32 &U, int x, int y,
+                                                          bool valid) {
     if (!(a.rm > 0.0f)) return 0u;
+    const int lane = threadIdx.x & 31;
     uint32_t hits = 0;
     for (int k = 0; k < a.n; k++) {
-        const float2 o = a.offs[k];
-        const float xg = xg_of(x, a.inv_zoom, o.x), yg = xg_of(y, a.inv_zoom, o.y);
-        const int i0 = f2i_floor(FG_FDIV(FG_FSUB(xg, a.rm), a.delta));
-        const int i1 = f2i_floor(FG_FDIV(FG_FADD(xg, a.rm), a.delta));
-        const int j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
-        const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
-        if (i0 > i1 || j0 > j1) continue;  // src/pixelwise.rs:60-62
-        const int ni = i1 - i0 + 1, nj = j1 - j0 + 1;
-        if (ni * nj > 64) {
-            hits += eval_regen(a, U, xg, yg, i0, i1, j0, j1) ? 1u : 0u;
-            continue;
-        }
-        // phase 1: bit (di * nj + dj) set when cell (i0 + di, j0 + dj) holds grains
+        float xg = 0.0f, yg = 0.0f;
+        int i0 = 0, j0 = 0, mid = 0;
         unsigned long long m = 0ull;
-        long long pix = -1, thresh = 0;
-        for (int di = 0; di < ni; di++) {
-            const int i = i0 + di;
-            const uint64_t colh = cell_col_hash(a.seed, i);
-            for (int dj = 0; dj < nj; dj++) {
-                const int j = j0 + dj;
-                const long long p = cell_pixel(a, i, j);
-                if (p != pix) {
-                    pix = p;
-                    thresh = a.cells[p].thresh;
+        bool hit = false;
+        if (valid) {
+            const float2 o = a.offs[k];
+            xg = xg_of(x, a.inv_zoom, o.x);
+            yg = xg_of(y, a.inv_zoom, o.y);
+            i0 = f2i_floor(FG_FDIV(FG_FSUB(xg, a.rm), a.delta));
+            const int i1 = f2i_floor(FG_FDIV(FG_FADD(xg, a.rm), a.delta));
+            j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
+            const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
+            if (i0 <= i1 && j0 <= j1) {  // else no cell (src/pixelwise.rs:60-62)
+                const int ni = i1 - i0 + 1, nj = j1 - j0 + 1;
+                if (ni > 8 || nj > 8) {
+                    hit = eval_regen(a, U, xg, yg, i0, i1, j0, j1);
+                } else {
+                    // phase 1
+                    mid = ((ni - 1) >> 1) * 8 + ((nj - 1) >> 1);
+                    long long pix = -1, thresh = 0;
+                    for (int di = 0; di < ni; di++) {
+                        const int i = i0 + di;
+                        const uint64_t colh = cell_col_hash(a.seed, i);
+                        for (int dj = 0; dj < nj; dj++) {
+                            const int j = j0 + dj;
+                            const long long p = cell_pixel(a, i, j);
+                            if (p != pix) {
+                                pix = p;
+                                thresh = a.cells[p].thresh;
+                            }
+                            const uint64_t h = cell_row_hash(colh, j);
+                            const uint64_t s0 = fmix64(h + kPhi), s3 = fmix64(h + 4 * kPhi);
+                            const long long v = (long long)((rotl64(s0 + s3, 23) + s0) >> 11);
+                            const int idx = di * 8 + dj;
+                            const int pos = idx == mid ? 0 : (idx == 0 ? mid : idx);
+                            if (v > thresh) m |= 1ull << pos;
+                        }
+                    }
                 }
-                const uint64_t h = cell_row_hash(colh, j);
-                const uint64_t s0 = fmix64(h + kPhi), s3 = fmix64(h + 4 * kPhi);
-                const long long v = (long long)((rotl64(s0 + s3, 23) + s0) >> 11);
-                if (v > thresh) m |= 1ull << (di * nj + dj);
             }
         }
-        // phase 2: the non-empty cells, middle first
-        const int mid = ((ni - 1) >> 1) * nj + ((nj - 1) >> 1);
-        bool hit = false;
-        if ((m >> mid) & 1ull) {
-            m &= ~(1ull << mid);
-            const int i = i0 + (ni - 1) / 2, j = j0 + (nj - 1) / 2;
-            hit = regen_cell(a, U, xg, yg, i, j, cell_col_hash(a.seed, i), a.cells[cell_pixel(a, i, j)]);
+        // phase 2: the warp's pairs, 32 at a time
+        const int cnt = __popcll((long long)m);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
         }
-        while (!hit && m != 0ull) {
-            const int t = __ffsll((long long)m) - 1;
-            m &= m - 1ull;
-            const int di = t / nj, i = i0 + di, j = j0 + (t - di * nj);
-            hit = regen_cell(a, U, xg, yg, i, j, cell_col_hash(a.seed, i), a.cells[cell_pixel(a, i, j)]);
+        const int tot = __shfl_sync(0xffffffffu, incl, 31);
+        for (int b = 0; b < tot; b += 32) {
+            const int p = b + lane;
+            int src = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int v = __shfl_sync(0xffffffffu, incl, src + step - 1);
+                if (v <= p) src += step;
+            }
+            src = min(src, 31);
+            int r = p - (__shfl_sync(0xffffffffu, incl, src) - __shfl_sync(0xffffffffu, cnt, src));
+            const unsigned mlo = __shfl_sync(0xffffffffu, (unsigned)m, src);
+            const unsigned mhi = __shfl_sync(0xffffffffu, (unsigned)(m >> 32), src);
+            const bool done = __shfl_sync(0xffffffffu, hit ? 1 : 0, src) != 0;
+            const float sx = __shfl_sync(0xffffffffu, xg, src), sy = __shfl_sync(0xffffffffu, yg, src);
+            const int si0 = __shfl_sync(0xffffffffu, i0, src), sj0 = __shfl_sync(0xffffffffu, j0, src);
+            const int smid = __shfl_sync(0xffffffffu, mid, src);
+            bool h = false;
+            if (p < tot && !done) {
+                // the r-th set bit of the owner's mask
+                unsigned word = mlo;
+                int base = 0;
+                const int c = __popc(mlo);
+                if (r >= c) {
+                    r -= c;
+                    word = mhi;
+                    base = 32;
+                }
+                int bit = 0;
+#pragma unroll
+                for (int half = 16; half > 0; half >>= 1) {
+                    const int cl = __popc(word & ((1u << half) - 1u));
+                    if (r >= cl) {
+                        r -= cl;
+                        bit += half;
+                        word >>= half;
+                    }
+                }
+                const int pos = base + bit;
+                const int idx = pos == 0 ? smid : (pos == smid ? 0 : pos);
+                const int i = si0 + (idx >> 3), j = sj0 + (idx & 7);
+                h = regen_cell(a, U, sx, sy, i, j, cell_col_hash(a.seed, i), a.cells[cell_pixel(a, i, j)]);
+            }
+            const unsigned hm = __reduce_or_sync(0xffffffffu, h ? (1u << src) : 0u);
+            hit = hit || ((hm >> lane) & 1u) != 0u;
         }
         hits += hit ? 1u : 0u;
     }
@@ -274,10 +330,15 @@ __device__ __forceinline__ void pixelwise_regen_pixels(const PixelwiseArgs &a, i
         dense = a.lam[(long long)yi * a.in_w + xi] * a.delta * a.delta > 0.6931472f;
     }
     const bool flat = __popc(__ballot_sync(0xffffffffu, dense)) >= 16;
-    if (x >= a.out_w) return;
+    const bool valid = x < a.out_w;
     const UniformF32 U = uniform_f32_new(0.0f, a.delta);
-    const uint32_t hits = flat ? pixelwise_pixel_flat(a, U, x, y) : pixelwise_pixel_split(a, U, x, y);
-    a.out[(long long)y * a.out_w + x] = (float)hits;
+    if (flat) {
+        if (!valid) return;
+        a.out[(long long)y * a.out_w + x] = (float)pixelwise_pixel_flat(a, U, x, y);
+    } else {
+        const uint32_t hits = pixelwise_pixel_split(a, U, x, y, valid);  // all 32 lanes
+        if (valid) a.out[(long long)y * a.out_w + x] = (float)hits;
+    }
 }
 
 // Block-wide exclusive scan of one int per thread (any blockDim.x that is a multiple of 32, <= 1024).
