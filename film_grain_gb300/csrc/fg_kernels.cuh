@@ -43,6 +43,11 @@ constexpr float kPwRegenDense = 0.4f;
 // samples reach fewer than kPwRegenKernel x its window's cells (and a sample's range fits 64 cells).
 constexpr int kPwRegenThreads = 256;
 constexpr float kPwRegenKernel = 1.5f;
+// Forms of the per-sample kernel by a warp's expected grains per cell (λδ²), from timings of uniform
+// planes (r 0.025-0.1, N 16-256): lane-major dealing up to 0.3, rank-major dealing up to 1.1 (u 0.7:
+// 11 % faster, u 0.9: 27 % faster than its neighbours), the flattened loop above (u 0.99).
+constexpr float kPwRegenRankLd = 0.3f;
+constexpr float kPwRegenFlatLd = 1.1f;
 
 struct PixelwiseArgs {
     const float *lam;           // in_w x in_h

@@ -127,12 +127,17 @@ static __device__ bool eval_regen(const PixelwiseArgs &a, const UniformF32 &U, f
 //      threshold, cell_count_h): the same short work on every lane, one column hash per column; the
 //      non-empty cells go to a 64-bit mask, cell (i0 + di, j0 + dj) at bit di * 8 + dj with the middle
 //      cell swapped into bit 0;
-//   2. the (lane, non-empty cell) pairs of the whole warp are dealt out 32 at a time: pair p goes to
-//      lane p % 32, which finds its owner by a shuffle binary search over the inclusive counts and the
-//      cell by a rank-select in the owner's mask, regenerates that cell's grains against the owner's
-//      sample and ORs a hit back to the owner (pairs of owners already covered are skipped).
+//   2. the (lane, non-empty cell) pairs of the whole warp are dealt out 32 at a time, each lane
+//      regenerating one cell's grains against its owner's sample and ORing a hit back to the owner.
+//      Lane-major order (kRankMajor false; sparse grains, few pairs): pair p goes to lane p % 32, which
+//      finds its owner by a shuffle binary search over the inclusive counts and the cell by a
+//      rank-select in the owner's mask (pairs of owners already covered are skipped).  Rank-major
+//      order (moderately dense grains): each round deals every uncovered lane's lowest pending cell,
+//      then their second cells, and so on, so that a sample covered by its middle cell drops out
+//      before the rest of its cells are dealt.
 // Coverage is an OR over the cells, so neither the order nor the dealing changes it.  A range wider
 // than 8 cells on an axis (outside the plane-level choice of this path) runs the plain loop instead.
+template <bool kRankMajor>
 __device__ __forceinline__ uint32_t pixelwise_pixel_split(const PixelwiseArgs &a, const UniformF32 &U, int x, int y,
                                                           bool valid) {
     if (!(a.rm > 0.0f)) return 0u;
@@ -180,59 +185,130 @@ __device__ __forceinline__ uint32_t pixelwise_pixel_split(const PixelwiseArgs &a
                 }
             }
         }
-        // phase 2: the warp's pairs, 32 at a time
-        const int cnt = __popcll((long long)m);
-        int incl = cnt;
+        if (kRankMajor) {
+            // phase 2: the warp's pairs, 32 per round in rank-major order: first every uncovered lane's
+            // lowest pending cell (the middle one when it holds grains), then their second cells, and so
+            // on, so that a covered sample drops out before its further cells are dealt.
+            for (;;) {
+                const bool live = m != 0ull && !hit;
+                const int mine = live ? __popcll((long long)m) : 0;
+                int owner = -1, rank = 0, before = 0, assigned = 0;
+                for (int r = 0; before < 32; r++) {
+                    const unsigned mask_r = __ballot_sync(0xffffffffu, mine > r);
+                    const int c = __popc(mask_r);
+                    if (c == 0) break;
+                    if (mine > r && before + __popc(mask_r & ((1u << lane) - 1u)) < 32) assigned++;
+                    if (owner < 0 && lane < before + c) {
+                        // the (lane - before)-th set bit of mask_r
+                        int q = lane - before, bit = 0;
+                        unsigned w = mask_r;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
-        }
-        const int tot = __shfl_sync(0xffffffffu, incl, 31);
-        for (int b = 0; b < tot; b += 32) {
-            const int p = b + lane;
-            int src = 0;
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1) {
-                const int v = __shfl_sync(0xffffffffu, incl, src + step - 1);
-                if (v <= p) src += step;
-            }
-            src = min(src, 31);
-            int r = p - (__shfl_sync(0xffffffffu, incl, src) - __shfl_sync(0xffffffffu, cnt, src));
-            const unsigned mlo = __shfl_sync(0xffffffffu, (unsigned)m, src);
-            const unsigned mhi = __shfl_sync(0xffffffffu, (unsigned)(m >> 32), src);
-            const bool done = __shfl_sync(0xffffffffu, hit ? 1 : 0, src) != 0;
-            const float sx = __shfl_sync(0xffffffffu, xg, src), sy = __shfl_sync(0xffffffffu, yg, src);
-            const int si0 = __shfl_sync(0xffffffffu, i0, src), sj0 = __shfl_sync(0xffffffffu, j0, src);
-            const int smid = __shfl_sync(0xffffffffu, mid, src);
-            bool h = false;
-            if (p < tot && !done) {
-                // the r-th set bit of the owner's mask
-                unsigned word = mlo;
-                int base = 0;
-                const int c = __popc(mlo);
-                if (r >= c) {
-                    r -= c;
-                    word = mhi;
-                    base = 32;
-                }
-                int bit = 0;
-#pragma unroll
-                for (int half = 16; half > 0; half >>= 1) {
-                    const int cl = __popc(word & ((1u << half) - 1u));
-                    if (r >= cl) {
-                        r -= cl;
-                        bit += half;
-                        word >>= half;
+                        for (int half = 16; half > 0; half >>= 1) {
+                            const int cl = __popc(w & ((1u << half) - 1u));
+                            if (q >= cl) {
+                                q -= cl;
+                                bit += half;
+                                w >>= half;
+                            }
+                        }
+                        owner = bit;
+                        rank = r;
                     }
+                    before += c;
                 }
-                const int pos = base + bit;
-                const int idx = pos == 0 ? smid : (pos == smid ? 0 : pos);
-                const int i = si0 + (idx >> 3), j = sj0 + (idx & 7);
-                h = regen_cell(a, U, sx, sy, i, j, cell_col_hash(a.seed, i), a.cells[cell_pixel(a, i, j)]);
+                if (before == 0) break;  // no lane has a pending cell
+                const int src = owner < 0 ? 0 : owner;
+                const unsigned mlo = __shfl_sync(0xffffffffu, (unsigned)m, src);
+                const unsigned mhi = __shfl_sync(0xffffffffu, (unsigned)(m >> 32), src);
+                const float sx = __shfl_sync(0xffffffffu, xg, src), sy = __shfl_sync(0xffffffffu, yg, src);
+                const int si0 = __shfl_sync(0xffffffffu, i0, src), sj0 = __shfl_sync(0xffffffffu, j0, src);
+                const int smid = __shfl_sync(0xffffffffu, mid, src);
+                bool h = false;
+                if (owner >= 0) {
+                    // the rank-th set bit of the owner's pending mask
+                    int r = rank;
+                    unsigned word = mlo;
+                    int base = 0;
+                    const int c = __popc(mlo);
+                    if (r >= c) {
+                        r -= c;
+                        word = mhi;
+                        base = 32;
+                    }
+                    int bit = 0;
+#pragma unroll
+                    for (int half = 16; half > 0; half >>= 1) {
+                        const int cl = __popc(word & ((1u << half) - 1u));
+                        if (r >= cl) {
+                            r -= cl;
+                            bit += half;
+                            word >>= half;
+                        }
+                    }
+                    const int pos = base + bit;
+                    const int idx = pos == 0 ? smid : (pos == smid ? 0 : pos);
+                    const int i = si0 + (idx >> 3), j = sj0 + (idx & 7);
+                    h = regen_cell(a, U, sx, sy, i, j, cell_col_hash(a.seed, i), a.cells[cell_pixel(a, i, j)]);
+                }
+                const unsigned hm = __reduce_or_sync(0xffffffffu, h ? (1u << src) : 0u);
+                hit = hit || ((hm >> lane) & 1u) != 0u;
+                for (int t = 0; t < assigned; t++) m &= m - 1ull;  // this round dealt the lowest `assigned` cells
             }
-            const unsigned hm = __reduce_or_sync(0xffffffffu, h ? (1u << src) : 0u);
-            hit = hit || ((hm >> lane) & 1u) != 0u;
+        } else {
+            // phase 2: the warp's pairs, 32 at a time in lane-major order
+            const int cnt = __popcll((long long)m);
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int tot = __shfl_sync(0xffffffffu, incl, 31);
+            for (int b = 0; b < tot; b += 32) {
+                const int p = b + lane;
+                int src = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int v = __shfl_sync(0xffffffffu, incl, src + step - 1);
+                    if (v <= p) src += step;
+                }
+                src = min(src, 31);
+                int r = p - (__shfl_sync(0xffffffffu, incl, src) - __shfl_sync(0xffffffffu, cnt, src));
+                const unsigned mlo = __shfl_sync(0xffffffffu, (unsigned)m, src);
+                const unsigned mhi = __shfl_sync(0xffffffffu, (unsigned)(m >> 32), src);
+                const bool done = __shfl_sync(0xffffffffu, hit ? 1 : 0, src) != 0;
+                const float sx = __shfl_sync(0xffffffffu, xg, src), sy = __shfl_sync(0xffffffffu, yg, src);
+                const int si0 = __shfl_sync(0xffffffffu, i0, src), sj0 = __shfl_sync(0xffffffffu, j0, src);
+                const int smid = __shfl_sync(0xffffffffu, mid, src);
+                bool h = false;
+                if (p < tot && !done) {
+                    // the r-th set bit of the owner's mask
+                    unsigned word = mlo;
+                    int base = 0;
+                    const int c = __popc(mlo);
+                    if (r >= c) {
+                        r -= c;
+                        word = mhi;
+                        base = 32;
+                    }
+                    int bit = 0;
+#pragma unroll
+                    for (int half = 16; half > 0; half >>= 1) {
+                        const int cl = __popc(word & ((1u << half) - 1u));
+                        if (r >= cl) {
+                            r -= cl;
+                            bit += half;
+                            word >>= half;
+                        }
+                    }
+                    const int pos = base + bit;
+                    const int idx = pos == 0 ? smid : (pos == smid ? 0 : pos);
+                    const int i = si0 + (idx >> 3), j = sj0 + (idx & 7);
+                    h = regen_cell(a, U, sx, sy, i, j, cell_col_hash(a.seed, i), a.cells[cell_pixel(a, i, j)]);
+                }
+                const unsigned hm = __reduce_or_sync(0xffffffffu, h ? (1u << src) : 0u);
+                hit = hit || ((hm >> lane) & 1u) != 0u;
+            }
         }
         hits += hit ? 1u : 0u;
     }
@@ -311,9 +387,9 @@ __device__ __forceinline__ uint32_t pixelwise_pixel_flat(const PixelwiseArgs &a,
 }
 
 // The per-sample path for the kPwRegenThreads pixels [x0, x0 + kPwRegenThreads) of row y (one per
-// thread of the CTA): each warp (32 neighbouring pixels) takes the dense form when most of its pixels
-// expect more than ln 2 grains per cell (over half the cells non-empty), else the sparse form, and
-// writes the hit counts.  Thread 0 adds the CTA's samples and the CTA to the diagnostics
+// thread of the CTA): each warp (32 neighbouring pixels) votes on its pixels' expected grains per cell
+// λδ² and takes the flattened form when most exceed kPwRegenFlatLd, the rank-major two-phase form when
+// most exceed kPwRegenRankLd, else the lane-major two-phase form, and writes the hit counts.  Thread 0 adds the CTA's samples and the CTA to the diagnostics
 // (regenerated samples, unstaged blocks, blocks).
 __device__ __forceinline__ void pixelwise_regen_pixels(const PixelwiseArgs &a, int x0, int y) {
     const int x = x0 + (int)threadIdx.x;
@@ -323,20 +399,22 @@ __device__ __forceinline__ void pixelwise_regen_pixels(const PixelwiseArgs &a, i
         atomicAdd(&a.diag[1], 1ull);
         atomicAdd(&a.diag[3], 1ull);
     }
-    bool dense = false;
+    float ld = 0.0f;  // expected grains per cell at this pixel
     if (x < a.out_w) {
         const int xi = min(a.in_w - 1, max(0, (int)floorf(((float)x + 0.5f) * a.inv_zoom)));
         const int yi = min(a.in_h - 1, max(0, (int)floorf(((float)y + 0.5f) * a.inv_zoom)));
-        dense = a.lam[(long long)yi * a.in_w + xi] * a.delta * a.delta > 0.6931472f;
+        ld = a.lam[(long long)yi * a.in_w + xi] * a.delta * a.delta;
     }
-    const bool flat = __popc(__ballot_sync(0xffffffffu, dense)) >= 16;
+    const bool flat = __popc(__ballot_sync(0xffffffffu, ld > kPwRegenFlatLd)) >= 16;
+    const bool rank_major = __popc(__ballot_sync(0xffffffffu, ld > kPwRegenRankLd)) >= 16;
     const bool valid = x < a.out_w;
     const UniformF32 U = uniform_f32_new(0.0f, a.delta);
     if (flat) {
         if (!valid) return;
         a.out[(long long)y * a.out_w + x] = (float)pixelwise_pixel_flat(a, U, x, y);
     } else {
-        const uint32_t hits = pixelwise_pixel_split(a, U, x, y, valid);  // all 32 lanes
+        const uint32_t hits = rank_major ? pixelwise_pixel_split<true>(a, U, x, y, valid)    // all 32 lanes
+                                         : pixelwise_pixel_split<false>(a, U, x, y, valid);
         if (valid) a.out[(long long)y * a.out_w + x] = (float)hits;
     }
 }
