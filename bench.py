@@ -11,8 +11,9 @@ planes).  Metric: MC samples/s = output pixels x channels x N per second.
   to pinned host u8 RGB (host colour split, lambda planes, H2D, kernels, fused colour, D2H).
 - ``roofline``: SM instruction issue (this path is integer/f32 ALU work: no dense contraction, almost
   no HBM traffic).  achieved = algorithmic lane-ops per launch / the launch's CUDA-event duration; the
-  lane-op count comes from oracle-counted per-grain quantities; peak = SMs x 128 lanes
-  x the SM clock sampled during the run.
+  lane-op count comes from per-grain quantities the oracle counts on a band of the same frame (grains,
+  x- and y-bounded pairs, centre hits; GW_COST below); peak = SMs x 128 lanes x the SM clock sampled
+  during the run.
 - ``cpu_baseline``: the CPU oracle (a C restatement of the reference's integrator, OpenMP over input
   rows as the reference's rayon loop) timed on bands of input rows of the same frame; its full-frame
   rate is extrapolated by grain count (work is proportional to grains).
@@ -249,7 +250,12 @@ def pixelwise_regen_lane_ops(lam, wl, derived, out_px):
     return terms
 
 
-# Algorithmic lane-ops of the grain-wise path (minimal exact implementation; derivation in the design doc).
+# Algorithmic lane-ops of the grain-wise path: the lane-op counts of a minimal exact implementation.
+# A grain: three xoshiro steps (~18 each), two uniforms (5 each), and for a lognormal radius the
+# ziggurat normal (~12) and a double-float exp (~70), plus clamps (~10): 150 (70 for a constant
+# radius).  A pair whose x bounds are tested: 2 adds, 2 subtracts, ceil, floor, 3 compares (10); whose
+# y bounds are tested too: 8 more; a centre hit: the disk test and the bit set (12).  Each output
+# pixel: its popcount pass (3 + 2 per mask word).
 GW_COST = dict(grain_lognorm=150, grain_const=70, x_pair=10, y_pair=8, hit=12, out_base=3, out_word=2)
 
 
@@ -341,17 +347,17 @@ def surrogate_compare(fg, sg, net, steps, warmup, plain_steps, clocks=None, seed
     conv_flop = px * 9 * sg.CH * sg.CH * 2
     conv_bytes = px * sg.CH * 2 * 2  # read h (the residual is the same tensor), write h'
 
-    judge = torch.empty_like(u_dev)
-    plain(1024, wl["seed"] + 1000, judge)()
+    ref1024 = torch.empty_like(u_dev)
+    plain(1024, wl["seed"] + 1000, ref1024)()
     # the method without the network at the network's cost: plain pixel-wise with N scaled to its time
     n_eq = max(1, int(round(256 * sur_ms / plain_ms)))
     plain_eq = torch.empty_like(u_dev)
     plain(n_eq, wl["seed"], plain_eq)()
     torch.cuda.synchronize()
-    q_sur = sg.evaluate(y, judge)
-    q_plain = sg.evaluate(plain256, judge)
-    q_eq = dict(sg.evaluate(plain_eq, judge), n_samples=n_eq)
-    q_id = sg.evaluate(u_dev, judge)
+    q_sur = sg.evaluate(y, ref1024)
+    q_plain = sg.evaluate(plain256, ref1024)
+    q_eq = dict(sg.evaluate(plain_eq, ref1024), n_samples=n_eq)
+    q_id = sg.evaluate(u_dev, ref1024)
 
     # end to end: pinned host u planes in, pinned host f32 planes out
     pin_u = torch.from_numpy(u_host).pin_memory()

@@ -1,6 +1,6 @@
 """The surrogate: a residual 3x3-conv network that stands in for the MC integrators in interactive
 previews.  No counterpart in the reference crate; the plain renders (render_pixelwise / render_grainwise)
-stay the method of record, produce its training targets and judge it.
+stay the method of record, produce its training targets and score it.
 
 Network (every conv 3x3, zero padding; weights bf16 on the tensor cores, f32 accumulation):
     x   = (u, N(0,1) noise, radius * radius_scale)          u = normalised intensity, radius in input px
