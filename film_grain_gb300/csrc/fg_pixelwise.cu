@@ -1,8 +1,11 @@
 // fg_pixelwise.cu -- the pixel-wise coverage estimator (src/pixelwise.rs:11-106) for sm_103a.
 //
 // The reference loops pixel -> offset sample -> cell -> grain and regenerates every cell's grains
-// from its cell_rng each time a sample visits it.  Here the work is regrouped by where the samples
-// land: sample (pixel x,y; offset k) has the input-space point
+// from its cell_rng each time a sample visits it.  A plane takes one of two kernels
+// (pixelwise_prefers_regen): the per-sample kernel keeps that loop, one thread per output pixel
+// (pixelwise_regen_pixels in fg_pixelwise.cuh), for planes whose samples reach fewer cells than a
+// staged window would hold (small radii, few samples per pixel); the block kernels regroup the work by
+// where the samples land: sample (pixel x,y; offset k) has the input-space point
 //     xg = ((x + 0.5) * inv_zoom) - offsets_input[k][0]      (same f32 rounding as src/pixelwise.rs:34)
 // and belongs to the block of input space [X0,X1) x [Y0,Y1) containing (xg, yg).  One CTA owns a
 // block; it
@@ -17,8 +20,9 @@
 // Because a cell's grains depend only on (seed, i, j) and coverage is an OR over the grains of the
 // sample's cells, the result equals the reference's early-exit loop bit for bit.  A block whose
 // window holds more grains than shared memory splits into quadrants (up to kPwMaxLevel levels);
-// samples whose cell range leaves the staged window (never expected) and leaf blocks that still
-// overflow fall back to the reference's per-sample regeneration, which is exact too.
+// border blocks (few owned samples), dense overflowing windows, samples whose cell range leaves the
+// staged window (never expected) and leaf blocks that still overflow run the reference's per-sample
+// regeneration instead, which is exact too.
 #include <algorithm>
 #include <cmath>
 
