@@ -120,9 +120,9 @@ static __device__ bool eval_regen(const PixelwiseArgs &a, const UniformF32 &U, f
 
 // Hit count of output pixel (x, y) over its N samples by the reference's per-sample loop
 // (src/pixelwise.rs:30-38 around evaluate_indicator, src/pixelwise.rs:47-106), for sparse and
-// moderately dense grains.  Called by all 32 lanes of a warp (neighbouring pixels; `valid` false for lanes past the row's end,
-// which take part without samples); the lanes take the samples in step, and each sample runs in two
-// phases:
+// moderately dense grains.  Called by all 32 lanes of a warp (neighbouring pixels; `valid` false for
+// lanes past the row's end, which take part without samples); the lanes take the samples in step, and
+// each sample runs in two phases:
 //   1. every cell of its range gets the emptiness test alone (the first uniform against the Poisson
 //      threshold, cell_count_h): the same short work on every lane, one column hash per column; the
 //      non-empty cells go to a 64-bit mask, cell (i0 + di, j0 + dj) at bit di * 8 + dj with the middle
