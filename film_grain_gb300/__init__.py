@@ -29,7 +29,7 @@ import numpy as np
 __all__ = [
     "RadiusDist", "Algo", "ColorMode", "MaxRadius", "Roi", "ParamsBuilder", "Params", "Derived", "RenderStats",
     "RenderError", "ParamsError", "CancelledError", "GpuError", "derive_common", "default_cell_delta",
-    "normalize_plane", "lambda_plane", "choose_algorithm", "render_pixelwise", "render_grainwise",
+    "normalize_plane", "lambda_plane", "lambda_from_plane", "choose_algorithm", "render_pixelwise", "render_grainwise",
     "render_with_input_image", "dry_run_with_input_image", "lib", "pixelwise_diagnostics", "pixelwise_kernel_count",
     "make_offsets",
     "Batch", "BatchTuning",
@@ -169,6 +169,7 @@ SIGNATURES = {
     "fg_default_cell_delta": (ctypes.c_float, [ctypes.c_float]),
     "fg_normalize_plane": (ctypes.c_float, [_vp, ctypes.c_int64, _vp]),
     "fg_lambda_plane": (None, [_vp, ctypes.c_int64, ctypes.c_float, _vp]),
+    "fg_lambda_from_plane": (ctypes.c_float, [_vp, ctypes.c_int64, ctypes.c_float, _vp]),
     "fg_render_pixelwise": (ctypes.c_int, [_vp, _P(_ParamsC), _P(_DerivedC), _vp, _vp, _vp, _vp]),
     "fg_render_grainwise": (ctypes.c_int, [_vp, _P(_ParamsC), _P(_DerivedC), _vp, _vp, _vp, _vp]),
     "fg_render_pixelwise_async": (ctypes.c_int, [_vp, _P(_ParamsC), _P(_DerivedC), _vp, _vp, _vp]),
@@ -359,6 +360,14 @@ def normalize_plane(plane: np.ndarray) -> Tuple[np.ndarray, float]:
     src = np.ascontiguousarray(plane, np.float32)
     dst = np.empty_like(src)
     mx = lib().fg_normalize_plane(src.ctypes.data, src.size, dst.ctypes.data)
+    return dst, mx
+
+
+def lambda_from_plane(plane: np.ndarray, inv_e_pi_r2: float) -> Tuple[np.ndarray, float]:
+    """lambda_plane(normalize_plane(plane)) in one host pass (bit-identical); returns (lambda, max)."""
+    src = np.ascontiguousarray(plane, np.float32)
+    dst = np.empty_like(src)
+    mx = lib().fg_lambda_from_plane(src.ctypes.data, src.size, inv_e_pi_r2, dst.ctypes.data)
     return dst, mx
 
 

@@ -472,15 +472,14 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
     } else {
         FG_CUDA(b_cells.alloc(mask_bytes * nplanes, s), "alloc sample masks");
     }
-    std::vector<float> norm(n_in), lam((size_t)n_in * nplanes);
+    std::vector<float> lam((size_t)n_in * nplanes);
     for (int c = 0; c < nplanes; c++) {
         if (cancelled(cancel)) {
             cudaStreamSynchronize(s);
             return set_error(FG_ERR_CANCELLED, "cancelled");
         }
         float *lc = lam.data() + (size_t)c * n_in;
-        normalize_plane(planes.data() + (size_t)c * n_in, (int64_t)n_in, norm.data());
-        lambda_plane(norm.data(), (int64_t)n_in, d.inv_e_pi_r2, lc);
+        lambda_from_plane(planes.data() + (size_t)c * n_in, (int64_t)n_in, d.inv_e_pi_r2, lc);
         FG_CUDA(cudaMemcpyAsync(d_lam + (size_t)c * n_in, lc, sizeof(float) * n_in, cudaMemcpyHostToDevice, s),
                 "lambda H2D");
         float *d_plane = d_out + (size_t)c * n_out;

@@ -226,17 +226,23 @@ int32_t choose_algorithm(const fg_params &p, const fg_derived &d) {
     return FG_ALGO_GRAIN;
 }
 
-// Parallel-for over [0, n) in contiguous chunks on the host's cores.
+// Chunks a parallel pass over n elements uses: one per host core, at least 65536 elements each.
+static int64_t chunk_count(int64_t n) {
+    unsigned hw = std::thread::hardware_concurrency();
+    return std::min<int64_t>(hw ? hw : 1, std::max<int64_t>(1, n / 65536));
+}
+
+// Parallel-for over [0, n) in chunk_count(n) contiguous chunks on the host's cores; f(t, b, e) runs
+// chunk t = [b, e).
 template <class F>
 static void parallel_chunks(int64_t n, F f) {
-    unsigned hw = std::thread::hardware_concurrency();
-    int64_t nt = std::min<int64_t>(hw ? hw : 1, std::max<int64_t>(1, n / 65536));
-    if (nt <= 1) { f(0, n); return; }
+    const int64_t nt = chunk_count(n);
+    if (nt <= 1) { f(0, 0, n); return; }
     std::vector<std::thread> th;
     int64_t per = (n + nt - 1) / nt;
     for (int64_t t = 0; t < nt; t++) {
         int64_t b = t * per, e = std::min(n, b + per);
-        if (b < e) th.emplace_back(f, b, e);
+        if (b < e) th.emplace_back(f, t, b, e);
     }
     for (auto &t : th) t.join();
 }
@@ -247,30 +253,57 @@ static inline float clampf(float x, float lo, float hi) {
     return x;
 }
 
-float normalize_plane(const float *src, int64_t n, float *dst) {
+// The plane's maximum as the reference folds it, fold(0.0, f32::max): f32::max (fmax) ignores NaN and
+// is commutative and associative, so per-chunk folds from 0.0 combined with fmax give the same value.
+static float plane_max(const float *src, int64_t n) {
+    std::vector<float> part((size_t)chunk_count(n), 0.0f);
+    parallel_chunks(n, [&](int64_t t, int64_t b, int64_t e) {
+        float m = 0.0f;
+        for (int64_t i = b; i < e; i++) m = std::fmax(m, src[i]);
+        part[(size_t)t] = m;
+    });
     float mx = 0.0f;
-    for (int64_t i = 0; i < n; i++) mx = std::fmax(mx, src[i]);
+    for (float m : part) mx = std::fmax(mx, m);
+    return mx;
+}
+
+static inline float normalized_value(float v, bool already, float den) {
+    return clampf(already ? v : v / den, 0.0f, 1.0f - kEps);
+}
+
+static inline float lambda_value(float norm, float inv_e_pi_r2) {
+    float c = clampf(norm, 0.0f, 1.0f - kEps);
+    float safe = std::fmax(1.0f - c, kEps);
+    float act = -inv_e_pi_r2 * std::log(safe);
+    return std::fmin(act, 1.0e6f);
+}
+
+float normalize_plane(const float *src, int64_t n, float *dst) {
+    const float mx = plane_max(src, n);
     const bool already = mx <= 1.0f + kEps;
     float den = mx + kEps;
     if (den < kEps) den = kEps;
-    parallel_chunks(n, [&](int64_t b, int64_t e) {
-        for (int64_t i = b; i < e; i++) {
-            float v = already ? src[i] : src[i] / den;
-            dst[i] = clampf(v, 0.0f, 1.0f - kEps);
-        }
+    parallel_chunks(n, [&](int64_t, int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; i++) dst[i] = normalized_value(src[i], already, den);
     });
     return mx;
 }
 
 void lambda_plane(const float *norm, int64_t n, float inv_e_pi_r2, float *dst) {
-    parallel_chunks(n, [&](int64_t b, int64_t e) {
-        for (int64_t i = b; i < e; i++) {
-            float c = clampf(norm[i], 0.0f, 1.0f - kEps);
-            float safe = std::fmax(1.0f - c, kEps);
-            float act = -inv_e_pi_r2 * std::log(safe);
-            dst[i] = std::fmin(act, 1.0e6f);
-        }
+    parallel_chunks(n, [&](int64_t, int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; i++) dst[i] = lambda_value(norm[i], inv_e_pi_r2);
     });
+}
+
+float lambda_from_plane(const float *src, int64_t n, float inv_e_pi_r2, float *dst) {
+    const float mx = plane_max(src, n);
+    const bool already = mx <= 1.0f + kEps;
+    float den = mx + kEps;
+    if (den < kEps) den = kEps;
+    parallel_chunks(n, [&](int64_t, int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; i++) dst[i] = lambda_value(normalized_value(src[i], already, den), inv_e_pi_r2);
+    });
+    return mx;
 }
 
 // load_luma_workspace / load_rgb_workspace (src/color.rs:158-213) from interleaved f32 RGB, with the
@@ -280,7 +313,7 @@ static inline float clamp01(float v) { return clampf(v, 0.0f, 1.0f); }
 void split_planes(const float *rgb, int64_t w, int64_t x0, int64_t y0, int64_t cw, int64_t ch, int luma,
                   float *p0, float *p1, float *p2) {
     const float YR = 0.2126f, YG = 0.7152f, YB = 0.0722f, CBD = 1.8556f, CRD = 1.5748f;
-    parallel_chunks(cw * ch, [&](int64_t b, int64_t e) {
+    parallel_chunks(cw * ch, [&](int64_t, int64_t b, int64_t e) {
         for (int64_t i = b; i < e; i++) {
             int64_t x = x0 + i % cw, y = y0 + i / cw;
             const float *px = rgb + 3 * (y * w + x);
@@ -323,6 +356,11 @@ FG_API float fg_default_cell_delta(float radius_mean) { return fg::default_cell_
 FG_API float fg_normalize_plane(const float *src, int64_t n, float *dst) {
     if (!src || !dst || n <= 0) return 0.0f;
     return fg::normalize_plane(src, n, dst);
+}
+
+FG_API float fg_lambda_from_plane(const float *src, int64_t n, float inv_e_pi_r2, float *dst) {
+    if (!src || !dst || n <= 0) return 0.0f;
+    return fg::lambda_from_plane(src, n, inv_e_pi_r2, dst);
 }
 
 FG_API void fg_lambda_plane(const float *normalized, int64_t n, float inv_e_pi_r2, float *dst) {

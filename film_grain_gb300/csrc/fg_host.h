@@ -18,6 +18,7 @@ fg_status derive(const fg_params &p, int64_t in_w, int64_t in_h, fg_derived *d, 
 int32_t choose_algorithm(const fg_params &p, const fg_derived &d);
 float normalize_plane(const float *src, int64_t n, float *dst);
 void lambda_plane(const float *norm, int64_t n, float inv_e_pi_r2, float *dst);
+float lambda_from_plane(const float *src, int64_t n, float inv_e_pi_r2, float *dst);
 void split_planes(const float *rgb, int64_t w, int64_t x0, int64_t y0, int64_t cw, int64_t ch, int luma, float *p0,
                   float *p1, float *p2);
 void fill_stats(const fg_params &p, const fg_derived &d, int32_t algo, fg_render_stats *s);

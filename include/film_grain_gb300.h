@@ -139,6 +139,11 @@ FG_API float fg_normalize_plane(const float *src, int64_t n, float *dst);
  * the platform logf; so does this library, to stay bit-identical). */
 FG_API void fg_lambda_plane(const float *normalized, int64_t n, float inv_e_pi_r2, float *dst);
 
+/* lambda_plane(normalize_plane(src)) in one pass (the same per-element operations, so the same bits),
+ * without the normalised plane in memory; returns the plane maximum as fg_normalize_plane does.  The
+ * crate runs the two steps in turn (src/lib.rs:140-166 via src/model.rs:228-265).  Host buffers. */
+FG_API float fg_lambda_from_plane(const float *src, int64_t n, float inv_e_pi_r2, float *dst);
+
 /* ---------------------------------------------------------------------------------------------
  * The integrators.
  * ------------------------------------------------------------------------------------------- */

@@ -98,6 +98,26 @@ def test_lambda_and_normalize_match_oracle(fgl, orc):
             assert np.array_equal(l1.view(np.uint32), l2.view(np.uint32))
 
 
+def test_lambda_planes_split_over_threads(fgl, orc):
+    """Planes large enough to be split over the host threads (per-chunk maxima), with values above 1
+    (the normalising branch), a negative value and a NaN: normalize + lambda, and the fused pass, against
+    the oracle bit for bit."""
+    rng = np.random.default_rng(5)
+    for scale in (1.0, 2.5):
+        plane = (rng.random((1024, 1031)) * scale).astype(np.float32)
+        plane[3, 5] = -0.25
+        plane[700, 9] = np.nan
+        plane[1023, 1030] = np.float32(scale * 1.01)  # the maximum sits in the last chunk
+        n1, m1 = fgl.normalize_plane(plane)
+        n2, m2 = orc.normalize_plane(plane)
+        assert m1 == m2 and np.array_equal(n1.view(np.uint32), n2.view(np.uint32))
+        for inv in (22.104853, 1e4):
+            l1 = fgl.lambda_plane(n1, inv)
+            assert np.array_equal(l1.view(np.uint32), orc.lambda_plane(n2, inv).view(np.uint32))
+            l3, m3 = fgl.lambda_from_plane(plane, inv)
+            assert m3 == m1 and np.array_equal(l3.view(np.uint32), l1.view(np.uint32))
+
+
 @pytest.mark.parametrize("kw,field", [
     (dict(radius_mean=0.0), "radius"), (dict(radius_mean=float("nan")), "radius"),
     (dict(radius_stddev=-1.0), "radius-stddev"), (dict(zoom=0.0), "zoom"), (dict(sigma_px=-2.0), "sigma"),
