@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -433,9 +434,10 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
     const int nplanes = luma ? 1 : 3;
     const size_t n_in = (size_t)cw * ch, n_out = (size_t)d.output_width * d.output_height;
 
-    std::vector<float> planes(3 * n_in);
-    split_planes(rgb, width, x0, y0, cw, ch, luma ? 1 : 0, planes.data(), planes.data() + n_in,
-                 planes.data() + 2 * n_in);
+    // host planes, written whole before they are read (no zero fill on the way to the first launch)
+    std::unique_ptr<float[]> planes(new float[3 * n_in]);
+    split_planes(rgb, width, x0, y0, cw, ch, luma ? 1 : 0, planes.get(), planes.get() + n_in,
+                 planes.get() + 2 * n_in);
     if (cancelled(cancel)) return set_error(FG_ERR_CANCELLED, "cancelled");
 
     keep_pool_memory();
@@ -461,7 +463,7 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
         FG_CUDA(b_cbcr.alloc(sizeof(float) * 2 * n_in, s), "alloc chroma");
         d_cb = (float *)b_cbcr.p;
         d_cr = d_cb + n_in;
-        FG_CUDA(cudaMemcpyAsync(d_cb, planes.data() + n_in, sizeof(float) * 2 * n_in, cudaMemcpyHostToDevice, s),
+        FG_CUDA(cudaMemcpyAsync(d_cb, planes.get() + n_in, sizeof(float) * 2 * n_in, cudaMemcpyHostToDevice, s),
                 "chroma H2D");
     }
     const size_t mask_bytes = algo == FG_ALGO_GRAIN ? grainwise_mask_bytes(p, d) : 0;
@@ -472,14 +474,14 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
     } else {
         FG_CUDA(b_cells.alloc(mask_bytes * nplanes, s), "alloc sample masks");
     }
-    std::vector<float> lam((size_t)n_in * nplanes);
+    std::unique_ptr<float[]> lam(new float[(size_t)n_in * nplanes]);
     for (int c = 0; c < nplanes; c++) {
         if (cancelled(cancel)) {
             cudaStreamSynchronize(s);
             return set_error(FG_ERR_CANCELLED, "cancelled");
         }
-        float *lc = lam.data() + (size_t)c * n_in;
-        lambda_from_plane(planes.data() + (size_t)c * n_in, (int64_t)n_in, d.inv_e_pi_r2, lc);
+        float *lc = lam.get() + (size_t)c * n_in;
+        lambda_from_plane(planes.get() + (size_t)c * n_in, (int64_t)n_in, d.inv_e_pi_r2, lc);
         FG_CUDA(cudaMemcpyAsync(d_lam + (size_t)c * n_in, lc, sizeof(float) * n_in, cudaMemcpyHostToDevice, s),
                 "lambda H2D");
         float *d_plane = d_out + (size_t)c * n_out;
