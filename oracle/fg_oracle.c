@@ -489,8 +489,10 @@ ORC_EXPORT int orc_choose_algorithm(const o_params *p, int32_t algo, float rm) {
 /* ------------------------------------------------------------------ pixel-wise (src/pixelwise.rs) */
 static inline float o_get_clamped(const float *lam, int64_t w, int64_t h, int64_t x, int64_t y) {
     if (w <= 0 || h <= 0) return 0.0f;
-    if (x < 0) x = 0; if (x > w - 1) x = w - 1;
-    if (y < 0) y = 0; if (y > h - 1) y = h - 1;
+    if (x < 0) x = 0;
+    if (x > w - 1) x = w - 1;
+    if (y < 0) y = 0;
+    if (y > h - 1) y = h - 1;
     return lam[y * w + x];
 }
 
@@ -571,8 +573,10 @@ static inline int o_bounds(float center, float radius, int32_t limit, int32_t *m
     if (limit <= 0) return 0;
     int32_t last = limit - 1;
     if (lo > last || hi < 0) return 0;
-    if (lo < 0) lo = 0; if (lo > last) lo = last;
-    if (hi < 0) hi = 0; if (hi > last) hi = last;
+    if (lo < 0) lo = 0;
+    if (lo > last) lo = last;
+    if (hi < 0) hi = 0;
+    if (hi > last) hi = last;
     if (lo > hi) return 0;
     *mn = lo; *mx = hi;
     return 1;
