@@ -609,8 +609,10 @@ ORC_EXPORT int orc_render_grainwise(const float *lam, const o_params *p, const o
     int64_t ix1 = (int64_t)ceilf(((float)ox1 - mnx + reach) / zoom) + 1;
     int64_t iy0 = (int64_t)floorf(((float)oy0 - mxy - reach) / zoom) - 1;
     int64_t iy1 = (int64_t)ceilf(((float)oy1 - mny + reach) / zoom) + 1;
-    if (ix0 < 0) ix0 = 0; if (iy0 < 0) iy0 = 0;
-    if (ix1 > d->in_w) ix1 = d->in_w; if (iy1 > d->in_h) iy1 = d->in_h;
+    if (ix0 < 0) ix0 = 0;
+    if (iy0 < 0) iy0 = 0;
+    if (ix1 > d->in_w) ix1 = d->in_w;
+    if (iy1 > d->in_h) iy1 = d->in_h;
 #ifdef _OPENMP
     if (threads > 0) omp_set_num_threads(threads);
 #endif
