@@ -1,7 +1,6 @@
 """The surrogate's CPU oracle checked on its own (no GPU): the backward pass against central finite
 differences in f64, bf16 rounding, Adam, and the spectrum metric on known signals."""
 import numpy as np
-import pytest
 
 from oracle import surrogate_ref as sr
 
