@@ -98,6 +98,20 @@ def test_lambda_and_normalize_match_oracle(fgl, orc):
             assert np.array_equal(l1.view(np.uint32), l2.view(np.uint32))
 
 
+def test_new_entry_points_reject_null_arguments(fgl):
+    """fg_pixelwise_kernel_count and fg_batch_kernel_count return FG_ERR_INVALID (4) on null arguments;
+    fg_lambda_from_plane on an empty plane returns 0 without touching memory."""
+    import ctypes
+    L = fgl.lib()
+    n = ctypes.c_int32(-1)
+    assert L.fg_pixelwise_kernel_count(None, None, None, ctypes.byref(n)) == 4 and n.value == -1
+    p = fgl.ParamsBuilder(radius_mean=0.1, n_samples=8, algo=fgl.Algo.Pixel).build()
+    d = fgl.derive_common(p, (16, 16))
+    assert L.fg_pixelwise_kernel_count(p.c, d._c, None, ctypes.byref(n)) == 4
+    assert L.fg_batch_kernel_count(None, ctypes.byref(n)) == 4
+    assert L.fg_lambda_from_plane(None, 0, 1.0, None) == 0.0
+
+
 def test_lambda_planes_split_over_threads(fgl, orc):
     """Planes large enough to be split over the host threads (per-chunk maxima), with values above 1
     (the normalising branch), a negative value and a NaN: normalize + lambda, and the fused pass, against
