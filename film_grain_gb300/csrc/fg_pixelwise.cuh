@@ -42,16 +42,12 @@ __device__ __forceinline__ uint64_t cell_row_hash(uint64_t col, int j) {
 }
 
 // Grain count of the cell with hash h; when q > 0 the stream is left positioned after the Poisson
-// draws.  q == 0 is decided from the first draw alone: only words 0 and 3 of the seeded state enter it.
+// draws.  q == 0 is decided from the first draw alone: only state words s0 and s3 (seed words 1, 2, 7
+// and 8) enter it.
 __device__ __forceinline__ uint32_t cell_count_h(uint64_t h, long long thresh, double exp_lambda, Xoshiro &rng) {
-    uint64_t s0 = fmix64(h + kPhi), s3 = fmix64(h + 4 * kPhi);
-    uint64_t r1 = rotl64(s0 + s3, 23) + s0;
-    long long v = (long long)(r1 >> 11);
+    const long long v = (long long)(small_first_u64(h) >> 11);
     if (v <= thresh) return 0u;
-    rng.s0 = s0;
-    rng.s1 = fmix64(h + 2 * kPhi);
-    rng.s2 = fmix64(h + 3 * kPhi);
-    rng.s3 = s3;
+    rng = small_seed(h);
     if (thresh >= 0) {
         (void)rng.next();  // the first draw, already evaluated
         return poisson_knuth_tail(u53_unit((uint64_t)v), exp_lambda, rng);
@@ -175,8 +171,7 @@ __device__ __forceinline__ uint32_t pixelwise_pixel_split(const PixelwiseArgs &a
                                 thresh = a.cells[p].thresh;
                             }
                             const uint64_t h = cell_row_hash(colh, j);
-                            const uint64_t s0 = fmix64(h + kPhi), s3 = fmix64(h + 4 * kPhi);
-                            const long long v = (long long)((rotl64(s0 + s3, 23) + s0) >> 11);
+                            const long long v = (long long)(small_first_u64(h) >> 11);
                             const int idx = di * 8 + dj;
                             const int pos = idx == mid ? 0 : (idx == 0 ? mid : idx);
                             if (v > thresh) m |= 1ull << pos;
@@ -649,8 +644,7 @@ __device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root
                             thresh = a.cells[p].thresh;
                         }
                         const uint64_t h = cell_row_hash(colh, wj0 + cj);
-                        const uint64_t s0 = fmix64(h + kPhi), s3 = fmix64(h + 4 * kPhi);
-                        const long long v = (long long)((rotl64(s0 + s3, 23) + s0) >> 11);
+                        const long long v = (long long)(small_first_u64(h) >> 11);
                         rc = cj * (int)Wc + ci;
                         nonempty = v > thresh;
                         if (!nonempty) S.pre[rc] = 0;

@@ -1,11 +1,13 @@
 // fg_rng.cuh -- the film_grain RNG streams and samplers, bit-identical on host and device.
 //
 // Restates src/rng.rs:1-52 and the third-party samplers it calls:
-//   rand 0.8.5     SmallRng = xoshiro256++ seeded by SplitMix64; next_u32 = high half of next_u64;
-//                  UniformFloat<f32> (23-bit mantissa draw); Standard f64 (53-bit multiply method);
-//                  Open01 f64 (52-bit transmute method).
-//   rand_core 0.6  SeedableRng::seed_from_u64 default (PCG32 output words fill the seed), used by
-//                  StdRng::seed_from_u64 in make_offsets (src/rng.rs:15).
+//   rand 0.8.5     SmallRng = xoshiro256++; next_u32 = high half of next_u64; UniformFloat<f32>
+//                  (23-bit mantissa draw); Standard f64 (53-bit multiply method); Open01 f64 (52-bit
+//                  transmute method).
+//   rand_core 0.6.4  SeedableRng::seed_from_u64 default (PCG32 output words fill the seed).  Both
+//                  SmallRng::seed_from_u64 (src/rng.rs:28,33; rand 0.8.5's SmallRng implements only
+//                  from_seed and from_rng, so the default applies) and StdRng::seed_from_u64 in
+//                  make_offsets (src/rng.rs:15) take it.
 //   rand_chacha    ChaCha12Rng = StdRng: ChaCha block function, 12 rounds, 64-bit counter, stream 0.
 //   rand_distr 0.4.3  Poisson (Knuth product below lambda 12, Cauchy-comparison rejection above,
 //                  Numerical Recipes' log-gamma), Normal via the 256-layer ziggurat, LogNormal.
@@ -18,8 +20,10 @@
 
 #if defined(__CUDACC__)
 #define FG_HD __host__ __device__ __forceinline__
+#define FG_HDC __host__ __device__ constexpr
 #else
 #define FG_HD inline
+#define FG_HDC constexpr
 #endif
 
 #ifdef __CUDA_ARCH__
@@ -81,16 +85,75 @@ struct Xoshiro {
         return r;
     }
 };
-// SmallRng::seed_from_u64: word i = fmix64(h + (i+1)*phi).  The four arguments differ, and fmix64 is
-// a bijection with fmix64(0) = 0, so at most one word can be zero: the all-zero-seed remap of
-// from_seed can never trigger and is omitted.
+// ---- SmallRng::seed_from_u64 (rand_core 0.6.4's default, which rand 0.8.5's SmallRng keeps)
+// The PCG32 LCG advances the state before each output; the XSH-RR output function turns state k
+// (k = 1..8) into seed word k; the eight words fill the 32-byte seed little-endian, and
+// Xoshiro256PlusPlus::from_seed reads it as four little-endian u64: s0 = w1 | w2 << 32, s1 = w3 | w4 << 32,
+// s2 = w5 | w6 << 32, s3 = w7 | w8 << 32.  An all-zero seed is replaced by
+// Xoshiro256PlusPlus::seed_from_u64(0) (SplitMix64 words fmix64(k * phi), k = 1..4).
+// State k is a jump-ahead of the input: M^k * h + I * (M^(k-1) + ... + M + 1) (mod 2^64), so the
+// words do not depend on each other and the emptiness tests compute only words 1, 2, 7 and 8.
+constexpr uint64_t kPcgMul = 6364136223846793005ull;
+constexpr uint64_t kPcgInc = 11634580027462260723ull;
+FG_HDC uint64_t pcg_jump_mul(int k) {
+    uint64_t a = 1;
+    for (int i = 0; i < k; i++) a *= kPcgMul;
+    return a;
+}
+FG_HDC uint64_t pcg_jump_add(int k) {
+    uint64_t c = 0;
+    for (int i = 0; i < k; i++) c = c * kPcgMul + kPcgInc;
+    return c;
+}
+FG_HDC uint64_t splitmix_word(int k) {  // fmix64(k * phi): word k-1 of seed_from_u64(0)
+    uint64_t z = (uint64_t)k * kPhi;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+FG_HD uint32_t rotr32(uint32_t x, uint32_t r) {
+#ifdef __CUDA_ARCH__
+    return __funnelshift_r(x, x, r);
+#else
+    r &= 31u;
+    return r ? (x >> r) | (x << (32u - r)) : x;
+#endif
+}
+// Seed word k (1..8) of seed_from_u64(h).
+template <int K>
+FG_HD uint32_t pcg_word(uint64_t h) {
+    constexpr uint64_t a = pcg_jump_mul(K), c = pcg_jump_add(K);
+    const uint64_t st = a * h + c;
+    return rotr32((uint32_t)(((st >> 18) ^ st) >> 27), (uint32_t)(st >> 59));
+}
+FG_HD uint64_t pcg_pair(uint32_t lo, uint32_t hi) { return (uint64_t)lo | ((uint64_t)hi << 32); }
+FG_HD Xoshiro small_seed_zero() {
+    Xoshiro x;
+    x.s0 = splitmix_word(1);
+    x.s1 = splitmix_word(2);
+    x.s2 = splitmix_word(3);
+    x.s3 = splitmix_word(4);
+    return x;
+}
 FG_HD Xoshiro small_seed(uint64_t h) {
     Xoshiro x;
-    x.s0 = fmix64(h + kPhi);
-    x.s1 = fmix64(h + 2 * kPhi);
-    x.s2 = fmix64(h + 3 * kPhi);
-    x.s3 = fmix64(h + 4 * kPhi);
+    x.s0 = pcg_pair(pcg_word<1>(h), pcg_word<2>(h));
+    x.s1 = pcg_pair(pcg_word<3>(h), pcg_word<4>(h));
+    x.s2 = pcg_pair(pcg_word<5>(h), pcg_word<6>(h));
+    x.s3 = pcg_pair(pcg_word<7>(h), pcg_word<8>(h));
+    if ((x.s0 | x.s1 | x.s2 | x.s3) == 0) return small_seed_zero();
     return x;
+}
+// The first next_u64 output of small_seed(h), from seed words 1, 2, 7 and 8 alone (the other two
+// state words enter only through the all-zero remap, checked when s0 and s3 are both zero).
+FG_HD uint64_t small_first_u64(uint64_t h) {
+    const uint64_t s0 = pcg_pair(pcg_word<1>(h), pcg_word<2>(h));
+    const uint64_t s3 = pcg_pair(pcg_word<7>(h), pcg_word<8>(h));
+    if ((s0 | s3) == 0) {
+        const Xoshiro x = small_seed(h);
+        return rotl64(x.s0 + x.s3, 23) + x.s0;
+    }
+    return rotl64(s0 + s3, 23) + s0;
 }
 // src/rng.rs:26-29 / 31-34
 FG_HD Xoshiro cell_rng(uint64_t seed, int32_t i, int32_t j) { return small_seed(mix3(seed, kCellStream, i, j)); }
@@ -455,12 +518,14 @@ FG_HD void chacha_block(const uint32_t key[8], uint64_t counter, uint64_t stream
 }
 FG_HD ChaCha12 chacha12_seed_from_u64(uint64_t state) {
     ChaCha12 c;
-    for (int i = 0; i < 8; i++) {
-        state = state * 6364136223846793005ull + 11634580027462260723ull;
-        uint32_t xs = (uint32_t)(((state >> 18) ^ state) >> 27);
-        uint32_t rot = (uint32_t)(state >> 59);
-        c.key[i] = rot ? ((xs >> rot) | (xs << (32u - rot))) : xs;
-    }
+    c.key[0] = pcg_word<1>(state);
+    c.key[1] = pcg_word<2>(state);
+    c.key[2] = pcg_word<3>(state);
+    c.key[3] = pcg_word<4>(state);
+    c.key[4] = pcg_word<5>(state);
+    c.key[5] = pcg_word<6>(state);
+    c.key[6] = pcg_word<7>(state);
+    c.key[7] = pcg_word<8>(state);
     c.block = 0;
     c.idx = 16;
     return c;

@@ -12,10 +12,15 @@
  * rand_chacha 0.3.1, rand_distr 0.4.3, statrs 0.16.1) exist in this environment, so the
  * third-party algorithms below are restated from their published definitions:
  *   - SplitMix64 finaliser (Steele/Lea/Flood), used by src/rng.rs:46-52 and by rand's
- *     Xoshiro256PlusPlus::seed_from_u64;
+ *     Xoshiro256PlusPlus::seed_from_u64 (reached only through the all-zero-seed remap of from_seed);
  *   - xoshiro256++ (Blackman & Vigna), rand 0.8.5's SmallRng on 64-bit targets; next_u32 takes the
  *     high 32 bits of next_u64;
- *   - rand_core 0.6.4 SeedableRng::seed_from_u64 default (PCG32 output function filling the seed);
+ *   - rand_core 0.6.4 SeedableRng::seed_from_u64 default (PCG32 output function filling the seed).
+ *     rand 0.8.5's SmallRng implements only from_seed and from_rng of SeedableRng, so
+ *     SmallRng::seed_from_u64 (src/rng.rs:28,33) is this default: eight PCG32 words written
+ *     little-endian into the 32-byte seed, then Xoshiro256PlusPlus::from_seed (four little-endian
+ *     u64 words; an all-zero seed is replaced by Xoshiro256PlusPlus::seed_from_u64(0)).  StdRng
+ *     (src/rng.rs:15) takes the same eight words as its ChaCha key;
  *   - ChaCha with 12 rounds, 64-bit block counter, stream 0 (rand_chacha 0.3.1 ChaCha12Rng = StdRng);
  *     the ChaCha block function alone IS pinned: tests check it at 20 rounds against OpenSSL's
  *     ChaCha20 keystream (vectors committed under tests/golden/);
@@ -88,10 +93,23 @@ static uint64_t o_mix3(uint64_t seed, uint64_t stream, int64_t a, int64_t b) {
     return o_splitmix64(o_rotl64(state + (uint64_t)b, 41));
 }
 
-/* xoshiro256++ with rand's SplitMix64 seed_from_u64 (SmallRng, src/rng.rs:26-34 call sites). */
+/* rand_core 0.6.4 SeedableRng::seed_from_u64 default: the state advances by the PCG32 LCG first,
+ * then the XSH-RR output function gives one u32 seed word (written little-endian). */
+static void o_pcg32_fill(uint64_t state, uint32_t words[8]) {
+    for (int i = 0; i < 8; i++) {
+        state = state * 6364136223846793005ull + 11634580027462260723ull;
+        uint32_t xorshifted = (uint32_t)(((state >> 18) ^ state) >> 27);
+        uint32_t rot = (uint32_t)(state >> 59);
+        words[i] = o_rotr32(xorshifted, rot);
+    }
+}
+
+/* xoshiro256++ (SmallRng, src/rng.rs:26-34 call sites). */
 typedef struct { uint64_t s[4]; } o_small_rng;
 
-static o_small_rng o_small_seed(uint64_t state) {
+/* Xoshiro256PlusPlus::seed_from_u64 of rand 0.8.5 (SplitMix64 fill); from_seed sends the all-zero
+ * seed here with state 0. */
+static o_small_rng o_xoshiro_splitmix_seed(uint64_t state) {
     o_small_rng r;
     for (int i = 0; i < 4; i++) {
         state += 0x9E3779B97F4A7C15ull;
@@ -100,7 +118,16 @@ static o_small_rng o_small_seed(uint64_t state) {
         z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
         r.s[i] = z ^ (z >> 31);
     }
-    if ((r.s[0] | r.s[1] | r.s[2] | r.s[3]) == 0) return o_small_seed(0); /* all-zero seed remap */
+    return r;
+}
+/* SmallRng::seed_from_u64 = rand_core's default: PCG32 words -> 32 seed bytes -> from_seed, which
+ * reads the bytes as four little-endian u64 (word 2k low, word 2k+1 high). */
+static o_small_rng o_small_seed(uint64_t state) {
+    uint32_t w[8];
+    o_pcg32_fill(state, w);
+    o_small_rng r;
+    for (int i = 0; i < 4; i++) r.s[i] = (uint64_t)w[2 * i] | ((uint64_t)w[2 * i + 1] << 32);
+    if ((r.s[0] | r.s[1] | r.s[2] | r.s[3]) == 0) return o_xoshiro_splitmix_seed(0); /* all-zero seed remap */
     return r;
 }
 static uint64_t o_small_next_u64(o_small_rng *r) {
@@ -149,15 +176,10 @@ static void o_chacha_block(const uint32_t key[8], uint64_t counter, uint64_t str
 /* StdRng = ChaCha12 keystream, consumed as consecutive little-endian u64 pairs. */
 typedef struct { uint32_t key[8]; uint64_t block; uint32_t buf[16]; int idx; } o_std_rng;
 
-/* rand_core 0.6.4 default seed_from_u64: PCG32 output words fill the 32-byte seed. */
+/* rand_core 0.6.4 default seed_from_u64: PCG32 output words fill the 32-byte seed (the ChaCha key). */
 static o_std_rng o_std_seed(uint64_t state) {
     o_std_rng r;
-    for (int i = 0; i < 8; i++) {
-        state = state * 6364136223846793005ull + 11634580027462260723ull;
-        uint32_t xorshifted = (uint32_t)(((state >> 18) ^ state) >> 27);
-        uint32_t rot = (uint32_t)(state >> 59);
-        r.key[i] = o_rotr32(xorshifted, rot);
-    }
+    o_pcg32_fill(state, r.key);
     r.block = 0;
     r.idx = 16;
     return r;

@@ -61,15 +61,37 @@ def test_splitmix_and_mix3_follow_rng_rs(orc):
         assert orc.mix3(seed, stream, a, b) == want
 
 
+def _pcg32_seed_words(state, n=8):
+    """rand_core 0.6.4 SeedableRng::seed_from_u64 default: advance the PCG32 LCG, then XSH-RR."""
+    words = []
+    for _ in range(n):
+        state = (state * 6364136223846793005 + 11634580027462260723) & M64
+        xorshifted = (((state >> 18) ^ state) >> 27) & 0xFFFFFFFF
+        rot = state >> 59
+        words.append(((xorshifted >> rot) | (xorshifted << ((32 - rot) & 31))) & 0xFFFFFFFF)
+    return words
+
+
+def _small_rng_py(h):
+    """SmallRng::seed_from_u64(h) of rand 0.8.5: its SeedableRng impl has only from_seed and from_rng,
+    so rand_core's default fills the 32-byte seed with PCG32 words (little-endian), and
+    Xoshiro256PlusPlus::from_seed reads four little-endian u64; an all-zero seed becomes
+    Xoshiro256PlusPlus::seed_from_u64(0), a SplitMix64 fill."""
+    seed = b"".join(w.to_bytes(4, "little") for w in _pcg32_seed_words(h))
+    s = [int.from_bytes(seed[8 * i:8 * i + 8], "little") for i in range(4)]
+    if not any(s):
+        st, s = 0, []
+        for _ in range(4):
+            st = (st + 0x9E3779B97F4A7C15) & M64
+            z = st
+            z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
+            z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
+            s.append(z ^ (z >> 31))
+    return s
+
+
 def _xoshiro_py(h, n):
-    s = []
-    st = h
-    for _ in range(4):
-        st = (st + 0x9E3779B97F4A7C15) & M64
-        z = st
-        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
-        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
-        s.append(z ^ (z >> 31))
+    s = _small_rng_py(h)
     out = []
     for _ in range(n):
         r = (_rotl((s[0] + s[3]) & M64, 23) + s[0]) & M64
@@ -80,9 +102,32 @@ def _xoshiro_py(h, n):
     return out
 
 
+def _mix3_py(seed, stream, a, b):
+    st = seed ^ stream
+    st = _splitmix_py(_rotl((st + (a & M64)) & M64, 17))
+    return _splitmix_py(_rotl((st + (b & M64)) & M64, 41))
+
+
 def test_xoshiro256pp_stream(orc):
     for h in (0, 7, 0xDEADBEEF, M64):
         assert [int(v) for v in orc.small_stream(h, 16)] == _xoshiro_py(h, 16)
+
+
+def test_cell_rng_first_outputs_follow_rand_core_default_seeding(orc):
+    """cell_rng(42, 0, 0) and neighbours (src/rng.rs:26-34), derived here from the published
+    rand_core 0.6.4 seed_from_u64 default and xoshiro256++ without the oracle's code; the oracle's
+    streams must agree word for word."""
+    cell, pixel = 0xA24B1C30BEBCCF59, 0x6935FA5C55F65F1B
+    for seed, i, j in ((42, 0, 0), (42, 1, 0), (42, 0, 1), (42, -3, 7), (7, 1023, 511), (0, 0, 0)):
+        want_cell = _xoshiro_py(_mix3_py(seed, cell, i, j), 8)
+        want_pixel = _xoshiro_py(_mix3_py(seed, pixel, i, j), 8)
+        assert [int(v) for v in orc.cell_stream(seed, i, j, False, 8)] == want_cell
+        assert [int(v) for v in orc.cell_stream(seed, i, j, True, 8)] == want_pixel
+    # the seed bytes are PCG32 words, not SplitMix64 words (rand 0.9 changed SmallRng to the latter)
+    h = _mix3_py(42, cell, 0, 0)
+    words = _pcg32_seed_words(h)
+    assert _small_rng_py(h)[0] == words[0] | (words[1] << 32)
+    assert _small_rng_py(h)[0] != _splitmix_py(h)
 
 
 def test_uniform_f32_scale_and_range(orc):
