@@ -1,22 +1,24 @@
 """Benchmark of the GB300 film-grain integrators (one JSON line on rank 0).
 
-Default workload (``--workload grain_rgb_1024``): plain grain-wise, RGB, 1024x1024x3 f32 input of 16
-seeded Gaussian blobs per channel over a 0.1 background, lognormal grain radius mean 0.05 px /
-std 0.025, filter sigma 0.8, N = 128, zoom 2 (2048^2 x 3 output).  A step renders one frame (three
-planes).  Metric: MC samples/s = output pixels x channels x N per second.
+Default workload (``--workload pixel_rgb_4096``, the largest single-GPU configuration): plain
+pixel-wise, RGB, 4096x4096x3 f32 input of 16 seeded Gaussian blobs per channel over a 0.1 background,
+lognormal grain radius mean 0.025 px / std 0.01, filter sigma 0.8, N = 256, zoom 1.  A step renders one
+frame (three planes).  Metric: MC samples/s = output pixels x channels x N per second.
 
-- ``value``: the three grain-wise launches per step on device-resident lambda planes (HBM), timed with
-  CUDA events around exactly K steps, L2 flushed (256 MiB write) before every step.
+- ``value``: the three pixel-wise render calls per step on device-resident lambda planes (HBM), timed
+  with CUDA events around exactly K steps, L2 flushed (256 MiB write) before every step.
 - ``e2e``: the same frame through the public C-ABI entry point fg_render_image from pinned host f32 RGB
   to pinned host u8 RGB (host colour split, lambda planes, H2D, kernels, fused colour, D2H).
 - ``roofline``: SM instruction issue (this path is integer/f32 ALU work: no dense contraction, almost
   no HBM traffic).  achieved = algorithmic lane-ops per launch / the launch's CUDA-event duration; the
-  lane-op count comes from per-grain quantities the oracle counts on a band of the same frame (grains,
-  x- and y-bounded pairs, centre hits; GW_COST below); peak = SMs x 128 lanes x the SM clock sampled
-  during the run.
-- ``cpu_baseline``: the CPU oracle (a C restatement of the reference's integrator, OpenMP over input
-  rows as the reference's rayon loop) timed on bands of input rows of the same frame; its full-frame
-  rate is extrapolated by grain count (work is proportional to grains).
+  lane-op count is a model of a minimal exact implementation (PW_COST / GW_COST below) evaluated on
+  quantities of the same frame; peak = SMs x 128 lanes x the SM clock sampled during the run.
+- ``cpu_baseline``: the CPU oracle (a C restatement of the reference's integrator, OpenMP over output
+  rows as the reference's rayon loop) timed on a band of output rows of the same frame.
+- ``configs``: the other benchmark configurations, each measured the same way with fewer steps
+  (default run at one GPU only): the 256^2 luma pixel-wise ramp, the 1024^2 x 3 -> 2048^2 x 3
+  grain-wise frame, the uneven 64-image sweep (batched graph vs per-image launches) and the surrogate
+  against the plain method on the 4096^2 x 3 frame.
 - ``--impl reference``: that CPU oracle alone, all host threads, each step one band.
 
 Multi-GPU (torchrun): every rank renders its own frame (replicas, weak scaling); value = all ranks'
@@ -194,20 +196,24 @@ def cpu_pixel_baseline(oracle, planes, wl, threads, rows=None):
     return samples / dt, dt, f"output rows {y0}..{y0 + r} of plane 0 ({samples} samples)", None
 
 
-# DRAM bytes per launch measured by ncu on the profiling cases (profiles/*_ncu.md), per unit of work:
-# sg_conv_fwd<32,32,residual>: 358.6 MB read+write for 3 x 1024^2 px; grainwise kernel: 18.25 MB for a
-# 1024^2-pixel output plane (the lambda plane plus the sample-mask lines that miss L2).
+# DRAM bytes per launch from ncu captures of the dominant kernels on their profiling cases (the
+# --profile-once runs), per unit of work: sg_conv_fwd<32,32,residual> on the 1024^2 x 3 surrogate input,
+# 358.6 MB read+write for 3 x 1024^2 px; grainwise_persistent_kernel on a 512^2 -> 1024^2 plane of the
+# grain-wise blob frame, 18.25 MB per 1024^2 output pixels (the lambda plane plus the sample-mask lines
+# that miss L2); the pixel-wise lean and deferred block passes on plane 0 of the 4096^2 x 3 frame,
+# 458.7 MB per 4096^2 output pixels.
 SG_CONV_DRAM_BYTES_PER_PX = 358.6e6 / (3 * 1024 * 1024)
 GRAINWISE_DRAM_BYTES_PER_OUT_PX = 18.25e6 / (1024 * 1024)
-
 PIXELWISE_DRAM_BYTES_PER_OUT_PX = (399.3e6 + 59.4e6) / (4096 * 4096)
 
 # Algorithmic lane-ops of the pixel-wise path (an exact method that hashes every cell once): per cell
-# the cell hash and first uniform (three SplitMix64 finalisers, ~62), per non-empty cell the Knuth
-# continuation (~60), per grain its generation (150 lognormal / 70 const), per sample its point and
-# cell range (~30), and ~8 per disk test, a sample testing the grains of its cell range until the first
-# hit (all of them when uncovered, half on average when covered).  Expectations from the lambda plane.
-PW_COST = dict(cell=62, nonempty=60, grain_lognorm=150, grain_const=70, sample=30, test=8)
+# its hash and first uniform (~65: the row stage of mix3, one SplitMix64, ~24; the four PCG32 seed words
+# that the first xoshiro256++ output needs, ~8 each; that output and the threshold compare, ~9), per
+# non-empty cell the Knuth continuation (~60), per grain its generation (150 lognormal / 70 const), per
+# sample its point and cell range (~30), and ~8 per disk test, a sample testing the grains of its cell
+# range until the first hit (all of them when uncovered, half on average when covered).  Expectations
+# from the lambda plane.
+PW_COST = dict(cell=65, nonempty=60, grain_lognorm=150, grain_const=70, sample=30, test=8)
 
 
 def pixelwise_lane_ops(lam, wl, derived, out_px):
@@ -232,7 +238,7 @@ def pixelwise_lane_ops(lam, wl, derived, out_px):
 # until a grain covers it.  Minimal lane-ops: a sample's set-up, one emptiness test per cell of its
 # range, and a Poisson draw plus the grains' generation and disk tests for each non-empty cell; the
 # early exit is credited as half the non-empty cells of a covered sample.
-PW_REGEN_COST = dict(sample=40, cell=45, nonempty=60, grain=30)
+PW_REGEN_COST = dict(sample=40, cell=65, nonempty=60, grain=30)
 
 
 def pixelwise_regen_lane_ops(lam, wl, derived, out_px):
@@ -381,40 +387,24 @@ def surrogate_compare(fg, sg, net, steps, warmup, plain_steps, clocks=None, seed
                 h2d=4 * px, d2h=4 * px, clocks=clk, launches_per_frame=3 + net.n_res, wl=wl, planes=planes)
 
 
-def run_surrogate(args, rank, world):
-    """--workload surrogate_rgb_4096: the surrogate against the plain method on the large frame."""
+def surrogate_line(steps, warmup, world, retrain=False, cpu=True):
+    """The surrogate against the plain method on the large frame (4096^2 x 3 blobs): returns the line."""
     import torch
     import film_grain_gb300 as fg
-    from film_grain_gb300 import build as fgbuild
     from film_grain_gb300 import surrogate as sg
-    fgbuild.build()
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    if args.profile_once:  # small case for ncu: the shipped network on a 1024^2 x 3 blob frame, twice
-        from film_grain_gb300 import workloads
-        net = sg.load_default()
-        planes = host_planes(workloads.blobs_rgb(1024, 1024, 1), "rgb")
-        u = torch.from_numpy(np.stack([fg.normalize_plane(p)[0] for p in planes])).cuda()
-        radius = torch.full((3,), 0.025, dtype=torch.float32, device="cuda")
-        for _ in range(2):
-            net.infer(u, radius, seed=7)
-        torch.cuda.synchronize()
-        log("profile-once: surrogate on 1024^2 x 3 rendered twice")
-        return
-    if args.retrain or not os.path.exists(sg.DEFAULT_WEIGHTS):
+    if retrain or not os.path.exists(sg.DEFAULT_WEIGHTS):
         net, info = sg.train_from_scratch(log=log)
         prov = dict(source="trained in this run", **info)
     else:
         net = sg.load_default()
         prov = dict(source="film_grain_gb300/weights/surrogate_c4.npz", **{k: (v.item() if hasattr(v, "item") else v)
                                                                            for k, v in net.meta.items()})
-    clocks = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
-    r = surrogate_compare(fg, sg, net, args.steps, args.warmup, plain_steps=min(args.steps, 3), clocks=clocks)
-    if rank != 0:
-        return
+    clocks = ClockSampler(torch.cuda.current_device())
+    r = surrogate_compare(fg, sg, net, steps, warmup, plain_steps=min(steps, 3), clocks=clocks)
     peaks, basis = _peaks()
     ach = r["conv_flop"] / (r["conv_ms"] / 1e3) / 1e12
     line = {"metric": "surrogate ms/frame (4096^2 RGB)", "value": r["sur_ms"], "unit": "ms/frame", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["sur_ms"], "higher_is_better": False,
+            "steps": steps, "warmup": warmup, "ms_per_step": r["sur_ms"], "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (f32 accumulate)",
             "data": "synthetic (seeded blob frame)",
             "config": {"workload": "surrogate_rgb_4096",
@@ -428,36 +418,35 @@ def run_surrogate(args, rank, world):
             "roofline": {"bound": "tensor", "achieved": ach, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                          "frac": ach / peaks["bf16_tflops"],
                          "traffic": SG_CONV_DRAM_BYTES_PER_PX * 3 * r["size"] ** 2,
-                         "traffic_basis": "ncu dram bytes of one 3x1024^2 launch "
-                                          "(profiles/sg_conv_fwd_surrogate_1024_ncu.md), scaled by pixels",
+                         "traffic_basis": "ncu dram bytes of sg_conv_fwd<32,32,residual> on the 1024^2 x 3 "
+                                          "surrogate input, scaled by pixels",
                          "kernel": "sg_conv_fwd<32,32,residual>", "launch_ms": r["conv_ms"],
                          "flop_per_launch": r["conv_flop"], "algorithmic_bytes_per_launch": r["conv_bytes"],
                          "hbm_frac": r["conv_bytes"] / (r["conv_ms"] / 1e3) / (peaks["hbm_gbs"] * 1e9),
                          "peak_basis": f"bf16 burst, {basis}"},
             "e2e": {"value": r["e2e_ms"], "unit": "ms/frame", "h2d_bytes_per_step": r["h2d"] + 12,
                     "d2h_bytes_per_step": r["d2h"], "path": "pinned f32 u planes -> fg_sg_infer -> pinned f32 planes"},
-            "gpu_launches": args.steps * r["launches_per_frame"], "clocks": r["clocks"]}
-    if not args.no_cpu_baseline:
+            "gpu_launches": steps * r["launches_per_frame"], "clocks": r["clocks"]}
+    if cpu:
         import oracle
         oracle.build()
         threads = os.cpu_count() or 1
-        rate, secs, desc, _ = cpu_pixel_baseline(oracle, r["planes"], r["wl"], threads, rows=2)
+        rate, secs, desc, _ = cpu_pixel_baseline(oracle, r["planes"], r["wl"], threads, rows=threads)
         frame = 3 * r["size"] * r["size"] * r["wl"]["n"]
         line["cpu_baseline"] = {"value": frame / rate * 1e3, "unit": "ms/frame", "cores": threads, "kind": "port",
                                 "sample": f"plain pixel-wise N=256 oracle on {desc}, extrapolated to the frame",
                                 "seconds": secs}
-    print(json.dumps(line), flush=True)
+    return line
 
 
-def run_batch(args, rank, world):
+def batch_line(steps, warmup, world):
     """The uneven sweep: 64 luma images (blob family), sizes over {128..2048}^2, radius over
     {0.025..0.2}, N over {16, 64, 256}, algorithm chosen per image by the crate's Auto rule.  value =
-    all images' samples / the autotuned batched graph's time; the per-image launch time is reported."""
+    all images' samples / the autotuned batched graph's time; the per-image launch time is reported,
+    and per size class the per-image time of those images alone."""
     import torch
     import film_grain_gb300 as fg
-    from film_grain_gb300 import build as fgbuild, workloads
-    fgbuild.build()
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from film_grain_gb300 import workloads
     L = fg.lib()
     specs = workloads.batched_sweep(64, seed=7)
     images, host_lam, samples = [], [], 0
@@ -476,33 +465,49 @@ def run_batch(args, rank, world):
     offs = [np.ascontiguousarray(im[2].offsets_input if im[3] == fg.Algo.Pixel else im[2].offsets, np.float32)
             for im in images]
 
-    def per_image():
-        for (lam, p, d, algo, _), o, of in zip(images, outs, offs):
+    def per_image(idx=None):
+        for k, ((lam, p, d, algo, _), o, of) in enumerate(zip(images, outs, offs)):
+            if idx is not None and k not in idx:
+                continue
             fn = L.fg_render_pixelwise_async if algo == fg.Algo.Pixel else L.fg_render_grainwise_async
             if fn(lam.data_ptr(), p.c, d._c, of.ctypes.data, o.data_ptr(), sp_) != 0:
                 raise RuntimeError(L.fg_last_error_message().decode())
 
-    def timed(fn, steps, warm):
+    def timed(fn, k, warm):
         for _ in range(warm):
             fn()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(steps):
+        for _ in range(k):
             fn()
         e1.record(stream)
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / steps
+        return e0.elapsed_time(e1) / k
 
-    t_per_image = timed(per_image, args.steps, args.warmup)
+    t_per_image = timed(per_image, steps, warmup)
+    classes = {}
+    for k, sp in enumerate(specs):
+        classes.setdefault(sp["size"], []).append(k)
+    by_size = {}
+    for size, idx in sorted(classes.items()):
+        ids = set(idx)
+        ms = timed(lambda: per_image(ids), max(1, steps // 2), 1)
+        by_size[str(size)] = {"images": len(idx), "per_image_ms": ms,
+                              "samples": sum(images[k][2].output_width * images[k][2].output_height * specs[k]["n"]
+                                             for k in idx)}
     b_default = fg.Batch(images)
-    t_default = timed(b_default.run, args.steps, args.warmup)
+    t_default = timed(b_default.run, steps, warmup)
     b_default.close()
     best, t_tune = fg.Batch.autotune(images)
     b = fg.Batch(images, best)
+    for size, idx in sorted(classes.items()):
+        sub = fg.Batch([images[k] for k in idx], best)
+        by_size[str(size)]["batched_ms"] = timed(sub.run, max(1, steps // 2), 1)
+        sub.close()
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
-    t_batch = timed(b.run, args.steps, args.warmup)
+    t_batch = timed(b.run, steps, warmup)
     clk = clocks.stop()
     # end to end: pinned lambda planes in, f32 planes out, around the batched graph
     pin_in = [torch.from_numpy(h).pin_memory() for h in host_lam]
@@ -514,102 +519,33 @@ def run_batch(args, rank, world):
         b.run()
         for o, po in zip(b.outputs, pin_out):
             po.copy_(o, non_blocking=True)
-    t_e2e = timed(e2e, args.steps, args.warmup)
+    t_e2e = timed(e2e, steps, warmup)
     h2d = sum(h.nbytes for h in host_lam)
     d2h = sum(o.numel() * 4 for o in b.outputs)
     line = {"metric": "MC samples/s", "value": samples / (t_batch / 1e3), "unit": "samples/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batch, "higher_is_better": True,
+            "steps": steps, "warmup": warmup, "ms_per_step": t_batch, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64-rng/f32", "data": "synthetic (seeded)",
             "config": {"workload": "batch_sweep_64", "images": len(images),
                        "pixel_images": sum(1 for im in images if im[3] == fg.Algo.Pixel),
                        "frame_samples": samples, "per_image_launch_ms": t_per_image,
                        "batched_default_ms": t_default, "batched_autotuned_ms": t_batch,
                        "speedup_vs_per_image": t_per_image / t_batch, "tuning": repr(best),
-                       "autotune_best_ms": t_tune, "l2": "inputs and scratch far larger than L2"},
+                       "autotune_best_ms": t_tune, "by_size": by_size,
+                       "l2": "inputs and scratch far larger than L2"},
             "e2e": {"value": samples / (t_e2e / 1e3), "unit": "samples/s", "ms_per_step": t_e2e,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "pinned lambda planes -> fg_batch_run -> pinned f32 planes"},
-            "gpu_launches": b.kernel_count * args.steps, "clocks": clk}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+            "gpu_launches": b.kernel_count * steps, "clocks": clk}
     b.close()
+    return line
 
 
-def run_reference(args, wl, rank):
-    import oracle
-    if rank != 0:
-        return
-    oracle.build()
-    threads = os.cpu_count() or 1
-    rgb = make_input(wl)
-    planes = host_planes(rgb, wl["mode"])
-    vals = []
-    desc = ""
-    for i in range(args.warmup + args.steps):
-        if wl["algo"] == "grain":
-            v, _, desc, _ = cpu_grain_baseline(oracle, planes, wl, threads, count=False)
-        else:
-            v, _, desc, _ = cpu_pixel_baseline(oracle, planes, wl, threads, rows=None if wl["w"] <= 256 else 2)
-        if i >= args.warmup:
-            vals.append(v)
-    value = statistics.median(vals)
-    line = {"impl": "reference", "metric": "MC samples/s", "value": value, "unit": "samples/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u64-rng/f32", "data": "synthetic (seeded)",
-            "config": {"workload": args.workload, "description": wl["desc"]},
-            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
-                             "sample": desc + "; each step one sample"},
-            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
-
-
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="grain_rgb_1024",
-                    choices=sorted(WORKLOADS) + ["batch_sweep_64", "surrogate_rgb_4096"])
-    ap.add_argument("--retrain", action="store_true",
-                    help="surrogate_rgb_4096: train the network in this run instead of loading the shipped weights")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-once", action="store_true",
-                    help="render plane 0 once after one warm-up render and exit (a small case for ncu captures)")
-    args = ap.parse_args()
-    args.warmup = max(3, args.warmup)
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    if args.workload == "batch_sweep_64":
-        if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the batched sweep has no reference counterpart"}))
-            return
-        run_batch(args, int(os.environ.get("RANK", "0")), world)
-        return
-    if args.workload == "surrogate_rgb_4096":
-        if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the surrogate has no reference counterpart"}))
-            return
-        run_surrogate(args, int(os.environ.get("RANK", "0")), world)
-        return
-    wl = WORKLOADS[args.workload]
-
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
-        run_reference(args, wl, rank)
-        return
-
+def plain_line(wl_name, steps, warmup, rank=0, world=1, dist=None, cpu=True, e2e_steps=None):
+    """One plain workload (WORKLOADS[wl_name]) through the per-plane render calls: returns the line
+    (rank 0) or None (other ranks)."""
     import torch
     import film_grain_gb300 as fg
-    from film_grain_gb300 import build as fgbuild
-    fgbuild.build()
-    torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
-
+    wl = WORKLOADS[wl_name]
     L = fg.lib()
     rgb = make_input(wl)
     params = build_params(fg, wl)
@@ -628,7 +564,7 @@ def main():
     launches_per_plane = 4 if wl["algo"] == "grain" else fg.pixelwise_kernel_count(params, derived)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    ev = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in planes] for _ in range(args.steps)]
+    ev = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in planes] for _ in range(steps)]
 
     def step(i=None):
         flush.fill_(1.0)
@@ -641,16 +577,7 @@ def main():
             if i is not None:
                 ev[i][c][1].record(stream)
 
-    if args.profile_once:
-        for _ in range(2):
-            rc = fn(lam_dev[0].data_ptr(), params.c, derived._c, offs.ctypes.data, outs[0].data_ptr(), sp)
-            if rc != 0:
-                raise RuntimeError(L.fg_last_error_message().decode())
-        torch.cuda.synchronize()
-        log(f"profile-once: {args.workload} plane 0 rendered twice")
-        return
-
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
 
@@ -662,14 +589,13 @@ def main():
     torch.cuda.synchronize()
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
-    launch_ms = []
     t_start.record(stream)
-    for i in range(args.steps):
+    for i in range(steps):
         step(i)
     t_end.record(stream)
     torch.cuda.synchronize()
-    for c in range(len(planes)):  # mean duration of plane c's launch over the timed steps
-        launch_ms.append(sum(ev[i][c][0].elapsed_time(ev[i][c][1]) for i in range(args.steps)) / args.steps)
+    launch_ms = [sum(ev[i][c][0].elapsed_time(ev[i][c][1]) for i in range(steps)) / steps
+                 for c in range(len(planes))]  # mean duration of plane c's render call
     elapsed = t_start.elapsed_time(t_end) / 1e3
     if dist:
         dist.barrier()
@@ -679,43 +605,42 @@ def main():
     clk = clocks.stop() if clocks else None
 
     samples_per_frame = ow * oh * len(planes) * wl["n"]
-    value = samples_per_frame * args.steps * world / elapsed
-    ms_per_step = elapsed / args.steps * 1e3
+    value = samples_per_frame * steps * world / elapsed
+    ms_per_step = elapsed / steps * 1e3
 
     # ---- end to end through the public entry point, pinned host buffers
+    e2e_steps = e2e_steps or steps
     pin_in = torch.from_numpy(rgb).pin_memory()
     pin_out = torch.empty((oh, ow, 3), dtype=torch.uint8).pin_memory()
     st = fg._StatsC()
     e2e_fn = lambda: L.fg_render_image(pin_in.data_ptr(), wl["w"], wl["h"], ctypes.byref(params.c), pin_out.data_ptr(),
                                        ctypes.byref(st), None, sp)
-    for _ in range(args.warmup):
+    for _ in range(min(warmup, 3)):
         assert e2e_fn() == 0, L.fg_last_error_message()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(e2e_steps):
         assert e2e_fn() == 0
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
     h2d = 4 * wl["w"] * wl["h"] * len(planes) + (16 if wl["algo"] == "grain" else 8) * wl["n"]
     if wl["mode"] == "luma":
         h2d += 8 * wl["w"] * wl["h"]
     d2h = 3 * ow * oh
 
     if rank != 0:
-        if dist:
-            dist.destroy_process_group()
-        return
+        return None
 
-    line = {"metric": "MC samples/s", "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+    line = {"metric": "MC samples/s", "value": value, "unit": "samples/s", "n_gpus": world, "steps": steps,
+            "warmup": warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64-rng/f32", "data": "synthetic (seeded, generated in bench.py)",
-            "config": {"workload": args.workload, "description": wl["desc"], "frame_samples": samples_per_frame,
+            "config": {"workload": wl_name, "description": wl["desc"], "frame_samples": samples_per_frame,
                        "ms_per_frame": ms_per_step, "l2": "256 MiB flush write before every step",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": samples_per_frame / e2e_s, "unit": "samples/s", "ms_per_frame": e2e_s * 1e3,
-                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": e2e_steps, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "fg_render_image: pinned f32 RGB in -> pinned u8 RGB out"},
-            "gpu_launches": args.steps * len(planes) * launches_per_plane,
+            "gpu_launches": steps * len(planes) * launches_per_plane,
             "clocks": clk}
 
     # ---- roofline of the dominant kernel and the CPU baseline
@@ -723,7 +648,7 @@ def main():
     f_mhz = (clk or {}).get("sm_mhz") or 2070.0
     peak = sm_count * 128 * f_mhz * 1e6  # lane-ops/s
     counts = None
-    if not args.no_cpu_baseline:
+    if cpu:
         import oracle
         oracle.build()
         threads = os.cpu_count() or 1
@@ -731,19 +656,19 @@ def main():
             cpu_v, cpu_t, desc, counts = cpu_grain_baseline(oracle, planes, wl, threads)
         else:
             cpu_v, cpu_t, desc, _ = cpu_pixel_baseline(oracle, planes, wl, threads,
-                                                        rows=None if wl["w"] <= 256 else 2)
+                                                        rows=None if wl["w"] <= 256 else threads)
         line["cpu_baseline"] = {"value": cpu_v, "unit": "samples/s", "cores": threads, "kind": "port",
                                 "sample": desc, "seconds": cpu_t}
+    peak_basis = f"{sm_count} SMs x 128 lanes x {f_mhz:.0f} MHz (sampled)"
     if counts and wl["algo"] == "grain":
         ops = [grainwise_lane_ops(c, wl, ow * oh) for c in counts]
         ach = sum(o / (ms / 1e3) for o, ms in zip(ops, launch_ms)) / len(ops)
         line["roofline"] = {"bound": "sm_issue", "achieved": ach / 1e12, "peak": peak / 1e12, "unit": "Tlane-op/s",
                             "frac": ach / peak, "traffic": GRAINWISE_DRAM_BYTES_PER_OUT_PX * ow * oh,
-                            "traffic_basis": "ncu dram bytes of the grain_rgb_512 launch "
-                                             "(profiles/grainwise_kernel_grain_rgb_512_ncu.md), scaled by output pixels",
+                            "traffic_basis": "ncu dram bytes of grainwise_persistent_kernel on a 512^2 -> 1024^2 "
+                                             "plane of the grain-wise blob frame, scaled by output pixels",
                             "kernel": "grainwise_persistent_kernel (launch_ms: the whole plane)", "launch_ms": launch_ms,
-                            "lane_ops_per_launch": ops, "counts": counts,
-                            "peak_basis": f"{sm_count} SMs x 128 lanes x {f_mhz:.0f} MHz (sampled)"}
+                            "lane_ops_per_launch": ops, "counts": counts, "peak_basis": peak_basis}
     if wl["algo"] == "pixel" and launches_per_plane == 3:
         ops = [pixelwise_regen_lane_ops(lh, wl, derived, ow * oh) for lh in lam_host]
         ach = sum(o["total"] / (ms / 1e3) for o, ms in zip(ops, launch_ms)) / len(ops)
@@ -751,19 +676,171 @@ def main():
                             "frac": ach / peak, "traffic": None,
                             "kernel": "pixelwise_regen_kernel (launch_ms: the whole plane)", "launch_ms": launch_ms,
                             "lane_ops_per_launch": [o["total"] for o in ops], "model_terms": ops[0],
-                            "peak_basis": f"{sm_count} SMs x 128 lanes x {f_mhz:.0f} MHz (sampled)"}
+                            "peak_basis": peak_basis}
     elif wl["algo"] == "pixel":
         ops = [pixelwise_lane_ops(lh, wl, derived, ow * oh) for lh in lam_host]
         ach = sum(o["total"] / (ms / 1e3) for o, ms in zip(ops, launch_ms)) / len(ops)
         line["roofline"] = {"bound": "sm_issue", "achieved": ach / 1e12, "peak": peak / 1e12, "unit": "Tlane-op/s",
                             "frac": ach / peak,
                             "traffic": PIXELWISE_DRAM_BYTES_PER_OUT_PX * ow * oh,
-                            "traffic_basis": "ncu dram bytes of the pixel_rgb_4096 launch "
-                                             "(profiles/pixelwise_kernel_pixel_rgb_4096_ncu.md), scaled by output pixels",
+                            "traffic_basis": "ncu dram bytes of the lean and deferred pixel-wise block passes on "
+                                             "plane 0 of the 4096^2 x 3 frame, scaled by output pixels",
                             "kernel": "pixelwise_kernel (launch_ms: the whole plane)", "launch_ms": launch_ms,
                             "lane_ops_per_launch": [o["total"] for o in ops], "model_terms": ops[0],
-                            "peak_basis": f"{sm_count} SMs x 128 lanes x {f_mhz:.0f} MHz (sampled)"}
-    print(json.dumps(line), flush=True)
+                            "peak_basis": peak_basis}
+    return line
+
+
+def profile_once(wl_name):
+    """Render plane 0 of a plain workload twice (one warm-up render, then the captured one): the small
+    case for ncu captures."""
+    import torch
+    import film_grain_gb300 as fg
+    wl = WORKLOADS[wl_name]
+    L = fg.lib()
+    params = build_params(fg, wl)
+    derived = fg.derive_common(params, (wl["w"], wl["h"]))
+    plane = host_planes(make_input(wl), wl["mode"])[0]
+    lam = torch.from_numpy(fg.lambda_plane(fg.normalize_plane(plane)[0], derived.inv_e_pi_r2)).cuda()
+    out = torch.empty((derived.output_height, derived.output_width), dtype=torch.float32, device="cuda")
+    offs = np.ascontiguousarray(derived.offsets if wl["algo"] == "grain" else derived.offsets_input, np.float32)
+    fn = L.fg_render_grainwise_async if wl["algo"] == "grain" else L.fg_render_pixelwise_async
+    for _ in range(2):
+        if fn(lam.data_ptr(), params.c, derived._c, offs.ctypes.data, out.data_ptr(),
+              torch.cuda.current_stream().cuda_stream) != 0:
+            raise RuntimeError(L.fg_last_error_message().decode())
+    torch.cuda.synchronize()
+    log(f"profile-once: {wl_name} plane 0 rendered twice")
+
+
+def profile_once_surrogate():
+    """The shipped network on a 1024^2 x 3 blob frame, twice: the small case for ncu captures."""
+    import torch
+    import film_grain_gb300 as fg
+    from film_grain_gb300 import surrogate as sg, workloads
+    net = sg.load_default()
+    planes = host_planes(workloads.blobs_rgb(1024, 1024, 1), "rgb")
+    u = torch.from_numpy(np.stack([fg.normalize_plane(p)[0] for p in planes])).cuda()
+    radius = torch.full((3,), 0.025, dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        net.infer(u, radius, seed=7)
+    torch.cuda.synchronize()
+    log("profile-once: surrogate on 1024^2 x 3 rendered twice")
+
+
+def reference_line(args, wl_name):
+    """--impl reference: the CPU oracle on the host cores, each step one bounded band of the frame."""
+    import oracle
+    oracle.build()
+    wl = WORKLOADS[wl_name]
+    threads = os.cpu_count() or 1
+    rgb = make_input(wl)
+    planes = host_planes(rgb, wl["mode"])
+    vals = []
+    desc = ""
+    for i in range(args.warmup + args.steps):
+        if wl["algo"] == "grain":
+            v, _, desc, _ = cpu_grain_baseline(oracle, planes, wl, threads, count=False)
+        else:
+            v, _, desc, _ = cpu_pixel_baseline(oracle, planes, wl, threads, rows=None if wl["w"] <= 256 else threads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    return {"impl": "reference", "metric": "MC samples/s", "value": value, "unit": "samples/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64-rng/f32", "data": "synthetic (seeded)",
+            "config": {"workload": wl_name, "description": wl["desc"]},
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
+                             "sample": desc + "; each step one sample"},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+DEFAULT_WORKLOAD = "pixel_rgb_4096"
+# The other benchmark configurations, measured in the default one-GPU run beside the headline.
+SIDE_WORKLOADS = ("pixel_luma_256", "grain_rgb_1024", "batch_sweep_64", "surrogate_rgb_4096")
+
+
+def side_configs(steps, warmup, cpu):
+    out = {}
+    for name in SIDE_WORKLOADS:
+        t0 = time.perf_counter()
+        try:
+            if name == "batch_sweep_64":
+                out[name] = batch_line(steps, warmup, 1)
+            elif name == "surrogate_rgb_4096":
+                out[name] = surrogate_line(steps, warmup, 1, cpu=cpu)
+            else:
+                out[name] = plain_line(name, steps, warmup, cpu=cpu)
+        except Exception as e:  # reported in the line, never silently dropped
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        out[name]["wall_s"] = time.perf_counter() - t0
+        log(f"side config {name}: {out[name]['wall_s']:.1f} s")
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
+                    choices=sorted(WORKLOADS) + ["batch_sweep_64", "surrogate_rgb_4096"])
+    ap.add_argument("--retrain", action="store_true",
+                    help="surrogate_rgb_4096: train the network in this run instead of loading the shipped weights")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other configurations measured beside the default workload")
+    ap.add_argument("--config-steps", type=int, default=5, help="timed steps of each side configuration")
+    ap.add_argument("--profile-once", action="store_true",
+                    help="render plane 0 once after one warm-up render and exit (a small case for ncu captures)")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if args.workload in ("batch_sweep_64", "surrogate_rgb_4096"):
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": f"{args.workload} has no reference counterpart"}))
+            return
+        if rank == 0:
+            print(json.dumps(reference_line(args, args.workload)), flush=True)
+        return
+
+    import torch
+    from film_grain_gb300 import build as fgbuild
+    fgbuild.build()
+    torch.cuda.set_device(local_rank)
+    if args.profile_once:
+        if args.workload == "surrogate_rgb_4096":
+            profile_once_surrogate()
+        elif args.workload != "batch_sweep_64":
+            profile_once(args.workload)
+        return
+    if args.workload == "batch_sweep_64":
+        line = batch_line(args.steps, args.warmup, world)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
+    if args.workload == "surrogate_rgb_4096":
+        line = surrogate_line(args.steps, args.warmup, world, retrain=args.retrain, cpu=not args.no_cpu_baseline)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    big = WORKLOADS[args.workload]["w"] * WORKLOADS[args.workload]["h"] >= 4096 * 4096
+    line = plain_line(args.workload, args.steps, args.warmup, rank, world, dist, cpu=not args.no_cpu_baseline,
+                      e2e_steps=min(args.steps, 5) if big else None)
+    if rank == 0 and world == 1 and args.workload == DEFAULT_WORKLOAD and not args.no_configs:
+        line["configs"] = side_configs(max(1, args.config_steps), 3, cpu=not args.no_cpu_baseline)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
 

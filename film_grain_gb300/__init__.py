@@ -21,6 +21,7 @@ from __future__ import annotations
 import ctypes
 import enum
 import os
+import threading
 from dataclasses import dataclass, field
 from typing import Callable, Optional, Tuple
 
@@ -388,20 +389,40 @@ def _is_torch_cuda(x) -> bool:
 
 
 class _Cancel:
-    """A cancel flag the library polls between launches (Fn() -> bool in the crate)."""
+    """The crate's cancel closure (Fn() -> bool, polled per row / pixel / grain in the CPU path) as the
+    flag the library reads: evaluated once before the call and, while the call runs, every millisecond
+    by a watcher thread that sets the flag when it returns True.  The library mirrors the flag into
+    the running kernels, which stop at their next work item."""
 
     def __init__(self, cancel: Optional[Callable[[], bool]]):
         self.flag = ctypes.c_int32(1 if (cancel is not None and cancel()) else 0)
+        self._stop = threading.Event()
+        self._thread = None
+        if cancel is not None and not self.flag.value:
+            def watch():
+                while not self._stop.wait(0.001):
+                    if cancel():
+                        self.flag.value = 1
+                        return
+            self._thread = threading.Thread(target=watch, name="fg-cancel-watch", daemon=True)
+            self._thread.start()
 
     @property
     def ptr(self):
         return ctypes.addressof(self.flag)
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._thread is not None:
+            self._thread.join()
+
 
 def _render(fn_name: str, lam, params: Params, derived: Derived, cancel, offs: np.ndarray):
     h, w = derived.input_height, derived.input_width
     oh, ow = derived.output_height, derived.output_width
-    cflag = _Cancel(cancel)
     fn = getattr(lib(), fn_name)
     if _is_torch_cuda(lam):
         import torch
@@ -409,15 +430,19 @@ def _render(fn_name: str, lam, params: Params, derived: Derived, cancel, offs: n
             raise RenderError("lambda must be a contiguous float32 tensor of input_width*input_height", _FG_INVALID)
         out = torch.empty((oh, ow), dtype=torch.float32, device=lam.device)
         stream = torch.cuda.current_stream(lam.device).cuda_stream
-        _raise(fn(lam.data_ptr(), ctypes.byref(params.c), ctypes.byref(derived._c), offs.ctypes.data,
-                  out.data_ptr(), cflag.ptr, stream))
+        with _Cancel(cancel) as cflag:
+            rc = fn(lam.data_ptr(), ctypes.byref(params.c), ctypes.byref(derived._c), offs.ctypes.data,
+                    out.data_ptr(), cflag.ptr, stream)
+        _raise(rc)
         return out
     src = np.ascontiguousarray(lam, np.float32)
     if src.size != w * h:
         raise RenderError("lambda plane size does not match the derived input size", _FG_INVALID)
     out = np.empty((oh, ow), np.float32)
-    _raise(fn(src.ctypes.data, ctypes.byref(params.c), ctypes.byref(derived._c), offs.ctypes.data, out.ctypes.data,
-              cflag.ptr, None))
+    with _Cancel(cancel) as cflag:
+        rc = fn(src.ctypes.data, ctypes.byref(params.c), ctypes.byref(derived._c), offs.ctypes.data, out.ctypes.data,
+                cflag.ptr, None)
+    _raise(rc)
     return out
 
 
@@ -465,9 +490,10 @@ def render_with_input_image(rgb: np.ndarray, params: Params, cancel: Optional[Ca
     ow, oh = _output_size(src.shape, params)
     out = np.empty((oh, ow, 3), np.uint8)
     st = _StatsC()
-    cflag = _Cancel(cancel)
-    _raise(lib().fg_render_image(src.ctypes.data, src.shape[1], src.shape[0], ctypes.byref(params.c),
-                                 out.ctypes.data, ctypes.byref(st), cflag.ptr, None))
+    with _Cancel(cancel) as cflag:
+        rc = lib().fg_render_image(src.ctypes.data, src.shape[1], src.shape[0], ctypes.byref(params.c),
+                                   out.ctypes.data, ctypes.byref(st), cflag.ptr, None)
+    _raise(rc)
     return out, _stats(st)
 
 

@@ -1,10 +1,14 @@
 // fg_capi.cu -- the render entry points of the C-ABI: buffer staging, launch planning and the
 // whole-image orchestration of render_from_workspace_impl (src/lib.rs:134-173).
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -41,6 +45,98 @@ bool is_device_ptr(const void *p) {
 }
 
 static bool cancelled(const volatile int32_t *cancel) { return cancel && *cancel != 0; }
+
+// ------------------------------------------------------------------ in-launch cancellation
+// The caller's cancel flag is ordinary host memory that the GPU cannot be assumed to reach, so while a
+// synchronous render runs a watcher thread polls it (every 200 us) and mirrors a non-zero value into
+// a word of mapped pinned memory that the kernels read (cancel_requested).  The words come from one
+// pinned block kept for the life of the process, one 64-byte line per render in flight.
+class CancelSlots {
+  public:
+    static CancelSlots &get() {
+        static CancelSlots s;
+        return s;
+    }
+    int *acquire() {
+        std::lock_guard<std::mutex> lock(mu_);
+        if (!base_) {
+            void *p = nullptr;
+            if (cudaHostAlloc(&p, kSlots * kLine, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess) {
+                cudaGetLastError();
+                return nullptr;  // no in-launch polling; the flag is still read between launches
+            }
+            base_ = static_cast<int *>(p);
+            for (int i = kSlots - 1; i >= 0; i--) free_.push_back(i);
+        }
+        if (free_.empty()) return nullptr;
+        int *w = base_ + free_.back() * (kLine / sizeof(int));
+        free_.pop_back();
+        ((volatile int *)w)[0] = 0;
+        ((volatile int *)w)[1] = 0;
+        return w;
+    }
+    void release(int *w) {
+        std::lock_guard<std::mutex> lock(mu_);
+        free_.push_back((int)((w - base_) / (kLine / sizeof(int))));
+    }
+
+  private:
+    static constexpr int kSlots = 256;
+    static constexpr size_t kLine = 64;
+    std::mutex mu_;
+    int *base_ = nullptr;
+    std::vector<int> free_;
+};
+
+class CancelWatch {
+  public:
+    explicit CancelWatch(const volatile int32_t *cancel) : cancel_(cancel) {
+        if (!cancel) return;
+        host_ = CancelSlots::get().acquire();
+        if (!host_) return;
+        void *d = nullptr;
+        if (cudaHostGetDevicePointer(&d, host_, 0) != cudaSuccess) {
+            cudaGetLastError();
+            CancelSlots::get().release(host_);
+            host_ = nullptr;
+            return;
+        }
+        dev_ = static_cast<int *>(d);
+        thread_ = std::thread([this] {
+            while (!done_.load(std::memory_order_acquire)) {
+                if (*cancel_ != 0) {
+                    ((volatile int *)host_)[0] = 1;
+                    return;
+                }
+                std::this_thread::sleep_for(std::chrono::microseconds(200));
+            }
+        });
+    }
+    // Called once the render's work on the GPU has finished (or failed).
+    ~CancelWatch() {
+        if (thread_.joinable()) {
+            done_.store(true, std::memory_order_release);
+            thread_.join();
+        }
+        if (host_) CancelSlots::get().release(host_);
+    }
+    CancelWatch(const CancelWatch &) = delete;
+    CancelWatch &operator=(const CancelWatch &) = delete;
+    int *dev() const { return dev_; }
+    // whether a CTA stopped on the flag
+    bool stopped() const { return host_ && ((volatile int *)host_)[1] != 0; }
+
+  private:
+    const volatile int32_t *cancel_;
+    int *host_ = nullptr;
+    int *dev_ = nullptr;
+    std::atomic<bool> done_{false};
+    std::thread thread_;
+};
+
+static fg_status cancelled_error(const CancelWatch &w) {
+    return set_error(FG_ERR_CANCELLED, w.stopped() ? "cancelled (stopped inside a kernel)" : "cancelled");
+}
 
 void offset_extents(const float *offs, uint32_t n, float ext[4]) {
     ext[0] = ext[1] = ext[2] = ext[3] = 0.0f;
@@ -137,13 +233,14 @@ struct DevBuf {
 
 fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_derived &d, const float *h_offs_in,
                             const float *d_offs_in, float *d_out, CellParam *d_cells, unsigned long long *d_diag,
-                            const EpilogueArgs *colour, cudaStream_t s, bool may_allocate) {
+                            const EpilogueArgs *colour, cudaStream_t s, bool may_allocate, int *d_cancel) {
     const int in_w = (int)d.input_width, in_h = (int)d.input_height;
     const int out_w = (int)d.output_width, out_h = (int)d.output_height;
     const PwPlan pl = plan_pixelwise(p, d, h_offs_in, 4);
     FG_CUDA(launch_cell_params(d_lam, in_w, in_h, d.delta, d_cells, s), "cell params");
     FG_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * (size_t)out_w * out_h, s), "memset");
-    const PixelwiseArgs a = pixelwise_args(p, d, pl, d_lam, d_cells, d_offs_in, d_out, d_diag);
+    PixelwiseArgs a = pixelwise_args(p, d, pl, d_lam, d_cells, d_offs_in, d_out, d_diag);
+    a.cancel = d_cancel;
     DevBuf defer;  // the lean pass's list of deferred root blocks (none without allocation: fat CTAs only)
     if (may_allocate) FG_CUDA(defer.alloc((2 + (size_t)pl.nbx * pl.nby) * sizeof(int), s), "alloc defer list");
     FG_CUDA(launch_pixelwise(a, pl.nby, static_cast<int *>(defer.p), s), "pixelwise kernel");
@@ -269,17 +366,26 @@ fg_status enqueue_grainwise_epilogue(const GrainwiseArgs &a, float *d_out, int m
     return FG_OK;
 }
 
+// The stream-ordered pool of the current device keeps its memory between renders (raised release
+// threshold), set once per device; safe to call from several threads.
 static void keep_pool_memory() {
-    static bool done = false;
-    if (done) return;
+    static std::atomic<bool> done[128];
+    static std::mutex mu;
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) {
+        cudaGetLastError();
+        return;
+    }
+    if (done[dev].load(std::memory_order_acquire)) return;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done[dev].load(std::memory_order_relaxed)) return;
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
         uint64_t thr = UINT64_MAX;
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
     }
-    done = true;
+    cudaGetLastError();
+    done[dev].store(true, std::memory_order_release);
 }
 
 // Shared body of the synchronous integrator entry points.
@@ -293,6 +399,7 @@ static fg_status render_plane_sync(int algo, const float *lambda, const fg_param
     cudaStream_t s = (cudaStream_t)stream;
     const fg_params &p = *params;
     const fg_derived &d = *derived;
+    CancelWatch watch(cancel);
     const size_t n_in = (size_t)d.input_width * d.input_height, n_out = (size_t)d.output_width * d.output_height;
     const size_t off_bytes = sizeof(float) * 2 * p.n_samples;
 
@@ -331,10 +438,11 @@ static fg_status render_plane_sync(int algo, const float *lambda, const fg_param
         FG_CUDA(b_diag.alloc(sizeof(unsigned long long) * 4, s), "alloc diag");
         FG_CUDA(cudaMemsetAsync(b_diag.p, 0, sizeof(unsigned long long) * 4, s), "memset diag");
         st = enqueue_pixelwise(d_lam, p, d, h_offs.data(), d_offs, d_out, (CellParam *)b_cells.p,
-                               (unsigned long long *)b_diag.p, nullptr, s);
+                               (unsigned long long *)b_diag.p, nullptr, s, true, watch.dev());
     } else {
         FG_CUDA(b_cells.alloc(grainwise_mask_bytes(p, d), s), "alloc sample masks");
         GrainwiseArgs a = grainwise_args(p, d, h_offs.data(), d_lam, d_offs, (unsigned int *)b_cells.p, kGrainMaskWords);
+        a.cancel = watch.dev();
         st = enqueue_grainwise(a, s);
         if (st == FG_OK) st = enqueue_grainwise_epilogue(a, d_out, 0, nullptr, nullptr, nullptr, s);
     }
@@ -346,7 +454,7 @@ static fg_status render_plane_sync(int algo, const float *lambda, const fg_param
     if (algo == FG_ALGO_PIXEL)
         FG_CUDA(cudaMemcpyAsync(g_pw_diag, b_diag.p, sizeof g_pw_diag, cudaMemcpyDeviceToHost, s), "diag D2H");
     FG_CUDA(cudaStreamSynchronize(s), "render");
-    if (cancelled(cancel)) return set_error(FG_ERR_CANCELLED, "cancelled");
+    if (cancelled(cancel)) return cancelled_error(watch);
     clear_error();
     return FG_OK;
 }
@@ -442,6 +550,7 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
 
     keep_pool_memory();
     cudaStream_t s = (cudaStream_t)stream;
+    CancelWatch watch(cancel);
     DevBuf b_lam, b_out, b_rgb8, b_cbcr, b_offs, b_cells, b_diag;
     FG_CUDA(b_lam.alloc(sizeof(float) * n_in * nplanes, s), "alloc lambda");
     FG_CUDA(b_out.alloc(sizeof(float) * n_out * nplanes, s), "alloc planes");
@@ -478,7 +587,7 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
     for (int c = 0; c < nplanes; c++) {
         if (cancelled(cancel)) {
             cudaStreamSynchronize(s);
-            return set_error(FG_ERR_CANCELLED, "cancelled");
+            return cancelled_error(watch);
         }
         float *lc = lam.get() + (size_t)c * n_in;
         lambda_from_plane(planes.get() + (size_t)c * n_in, (int64_t)n_in, d.inv_e_pi_r2, lc);
@@ -494,10 +603,11 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
                 e.mode = 2; e.out_rgb8 = (unsigned char *)b_rgb8.p; e.p0 = d_out; e.p1 = d_out + n_out;
             }
             st = enqueue_pixelwise(d_lam + (size_t)c * n_in, p, d, offs_in.data(), (const float *)b_offs.p, d_plane,
-                                   (CellParam *)b_cells.p, (unsigned long long *)b_diag.p, &e, s);
+                                   (CellParam *)b_cells.p, (unsigned long long *)b_diag.p, &e, s, true, watch.dev());
         } else {
             unsigned int *plane_mask = (unsigned int *)((unsigned char *)b_cells.p + mask_bytes * c);
             GrainwiseArgs a = grainwise_args(p, d, offs.data(), d_lam + (size_t)c * n_in, b_offs.p, plane_mask, kGrainMaskWords);
+            a.cancel = watch.dev();
             st = enqueue_grainwise(a, s);
             if (st == FG_OK && c == nplanes - 1) {
                 a.gmask = (unsigned int *)b_cells.p;  // all planes' masks, consecutive
@@ -511,7 +621,7 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
     }
     FG_CUDA(cudaMemcpyAsync(out_rgb8, b_rgb8.p, 3 * n_out, cudaMemcpyDeviceToHost, s), "rgb8 D2H");
     FG_CUDA(cudaStreamSynchronize(s), "render");
-    if (cancelled(cancel)) return set_error(FG_ERR_CANCELLED, "cancelled");
+    if (cancelled(cancel)) return cancelled_error(watch);
     if (stats) fill_stats(p, d, algo, stats);
     clear_error();
     return FG_OK;

@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(kGwThreads, 2) grainwise_persistent_kernel(con
     for (;;) {
         if (threadIdx.x == 0) {
             const int i = atomicAdd(a.work, 1);  // item i: part i % parts of the (i / parts)-th tile
-            s_tile = i < ntiles * parts ? i : -1;
+            s_tile = (i < ntiles * parts && !cancel_requested(a.cancel)) ? i : -1;
         }
         __syncthreads();
         const int i = s_tile;

@@ -22,7 +22,8 @@ PixelwiseArgs pixelwise_args(const fg_params &p, const fg_derived &d, const PwPl
                              const CellParam *d_cells, const float *d_offs_in, float *d_out, unsigned long long *d_diag);
 fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_derived &d, const float *h_offs_in,
                             const float *d_offs_in, float *d_out, CellParam *d_cells, unsigned long long *d_diag,
-                            const EpilogueArgs *colour, cudaStream_t s, bool may_allocate = true);
+                            const EpilogueArgs *colour, cudaStream_t s, bool may_allocate = true,
+                            int *d_cancel = nullptr);
 // The grain-wise offset table: n entries (frac(offy), offx, offy, k) sorted by frac(offx), followed by
 // the bucket index over frac(offx) (kGwBucketCount + 1 ints).
 size_t grain_table_bytes(uint32_t n);

@@ -49,6 +49,18 @@ constexpr float kPwRegenKernel = 1.5f;
 constexpr float kPwRegenRankLd = 0.3f;
 constexpr float kPwRegenFlatLd = 1.1f;
 
+// In-launch cancellation: `cancel` is null or two words of mapped pinned host memory.  Word 0 is set
+// by the library's host watcher once the caller's cancel flag turns non-zero; the persistent passes
+// read it once per work item they pull (the block passes once per block) and stop, and a CTA that
+// stops on it sets word 1.
+#ifdef __CUDACC__
+__device__ __forceinline__ bool cancel_requested(int *cancel) {
+    if (!cancel || *(volatile int *)cancel == 0) return false;
+    *(volatile int *)(cancel + 1) = 1;
+    return true;
+}
+#endif
+
 struct PixelwiseArgs {
     const float *lam;           // in_w x in_h
     const CellParam *cells;     // in_w x in_h
@@ -66,6 +78,7 @@ struct PixelwiseArgs {
     int lognorm;
     float radius_mean;
     double log_mu, log_sigma;
+    int *cancel;                // null, or the in-launch cancellation words (cancel_requested)
 };
 
 constexpr int kGwBucketCount = 256;  // bucket index over the frac(offx)-sorted offsets
@@ -88,6 +101,7 @@ struct GrainwiseArgs {
     double log_mu, log_sigma;
     int *work;                  // null: one CTA per tile; else the tile scheduler's area (grainwise_work_ints)
     int parts;                  // CTAs per tile (>= 1; above 1 only for the bitmask variants)
+    int *cancel;                // null, or the in-launch cancellation words (cancel_requested)
 };
 
 // popcount / colour epilogue of the grain-wise path.

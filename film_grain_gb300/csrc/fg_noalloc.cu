@@ -11,10 +11,14 @@
 //
 // The host side only ever uses the array through the device address that cudaGetSymbolAddress
 // returns for the current device (the symbol itself is a host-side stand-in, not a device address).
-// That address is looked up on the first call made on each device and cached.
+// That address is looked up on the first call made on each device and cached together with the
+// unique ID of the CUDA context it belongs to; when the device's context is later destroyed and
+// recreated (cudaDeviceReset, or another context made current), the ID changes and the next call
+// looks the address up again instead of using a stale one.
 #include <mutex>
 #include <string>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "../../include/film_grain_gb300.h"
@@ -32,23 +36,60 @@ constexpr size_t kNaScratchBytes = kNaCellsBytes + kNaOffsBytes + kNaDiagBytes;
 // The shared scratch of every fg_render_pixelwise_noalloc call on a device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaScratchBytes];
 
+struct NoallocSlot {
+    unsigned long long ctx_id;  // context the address belongs to (0: unknown, look up on every call)
+    unsigned char *ptr;
+};
 static std::mutex g_noalloc_mu;
-static unsigned char *g_noalloc_ptr[128];  // device address of the array, per device ordinal
+static NoallocSlot g_noalloc_slot[128];  // per device ordinal
 
-// Device address of the scratch array on the current device, looked up once per device.
+// Unique ID of the calling thread's current CUDA context (0 when there is none or the driver
+// entry points are unavailable).  The driver functions are reached through the runtime, so the
+// library needs no link against the driver library.
+static unsigned long long current_context_id() {
+    typedef CUresult (*GetCurrentFn)(CUcontext *);
+    typedef CUresult (*GetIdFn)(CUcontext, unsigned long long *);
+    static GetCurrentFn get_current = nullptr;
+    static GetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetIdFn>(f);
+        cudaGetLastError();
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+    if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array on the current device and context, looked up once per
+// device (again after its context changes).
 static fg_status noalloc_scratch(unsigned char **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
     if (dev < 0 || dev >= 128) return set_error(FG_ERR_UNSUPPORTED, "device ordinal out of range");
+    const unsigned long long id = current_context_id();
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    NoallocSlot &slot = g_noalloc_slot[dev];
+    if (!slot.ptr || id == 0 || slot.ctx_id != id) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress of the scratch array");
-        g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
+        slot.ptr = static_cast<unsigned char *>(p);
+        slot.ctx_id = id ? id : current_context_id();  // the lookup made the device's context current
     }
-    *out = g_noalloc_ptr[dev];
+    *out = slot.ptr;
     return FG_OK;
 }
 

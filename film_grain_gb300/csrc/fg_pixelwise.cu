@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(PwFat::kThreads, PwFat::kCtasPerSm)
     for (;;) {
         if (threadIdx.x == 0) {
             const int i = atomicAdd(defer - 1, 1);
-            s_id = i < n ? defer[1 + i] : -1;
+            s_id = (i < n && !cancel_requested(a.cancel)) ? defer[1 + i] : -1;
         }
         __syncthreads();
         const int id = s_id;
@@ -103,6 +103,11 @@ __global__ void __launch_bounds__(PwFat::kThreads, PwFat::kCtasPerSm)
 // barriers.  CTA b covers pixels [256 (b % row_ctas), +256) of row b / row_ctas.
 __global__ void __launch_bounds__(kPwRegenThreads) pixelwise_regen_kernel(const __grid_constant__ PixelwiseArgs a,
                                                                           int row_ctas) {
+    if (a.cancel) {  // once per warp: the warp's lanes work in step, so the whole warp stops
+        int stop = 0;
+        if ((threadIdx.x & 31) == 0) stop = cancel_requested(a.cancel) ? 1 : 0;
+        if (__shfl_sync(0xffffffffu, stop, 0)) return;
+    }
     pixelwise_regen_pixels(a, (int)(blockIdx.x % (unsigned)row_ctas) * kPwRegenThreads,
                            (int)(blockIdx.x / (unsigned)row_ctas));
 }

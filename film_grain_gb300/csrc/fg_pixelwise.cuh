@@ -462,6 +462,7 @@ struct PwShared {
     int fx0, fx1, fy0, fy1;               // owned-pixel footprint
     int nsamples;
     float est_grains, est_cells;          // lean pass: expected grains / non-empty cells of the window
+    int stop;                             // cancellation seen: the block stops
 };
 
 
@@ -477,6 +478,9 @@ __device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root
     const bool lean = C::kDefers && may_defer;
     bool deferred = false;
     const UniformF32 U = uniform_f32_new(0.0f, a.delta);
+    // the cancellation word, read now and tested after the ownership pass (its latency overlaps it)
+    int cancel_seen = 0;
+    if (tid == 0 && a.cancel) cancel_seen = *(volatile int *)a.cancel;
 
     if (tid == 0) {
         S.sp = 1;
@@ -585,8 +589,15 @@ __device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root
                 atomicMin(&S.fy0, ly0); atomicMax(&S.fy1, ly1);
             }
         }
+        if (tid == 0) {
+            S.stop = cancel_seen;
+            if (cancel_seen) {
+                S.sp = 0;  // drop the block's remaining quadrants too
+                *(volatile int *)(a.cancel + 1) = 1;
+            }
+        }
         __syncthreads();
-        if (S.nsamples == 0) continue;
+        if (S.nsamples == 0 || S.stop) continue;
         const int fx0 = S.fx0, fy0 = S.fy0, fw = S.fx1 - S.fx0, fh = S.fy1 - S.fy0;
         const bool use_cnt = (long long)fw * fh <= kPwFootMax;
 

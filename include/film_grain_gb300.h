@@ -176,9 +176,13 @@ FG_API fg_status fg_render_grainwise_async(const float *d_lambda, const fg_param
  * is host memory.  The kernel's scratch is one fixed-size array compiled into this library (present
  * on every GPU that loads it, until process exit), so the call is limited to input planes of at
  * most FG_NOALLOC_MAX_INPUT_PIXELS pixels and N <= FG_NOALLOC_MAX_SAMPLES (FG_ERR_UNSUPPORTED
- * beyond).  The first call on each device looks up the array's device address; make that first call
- * before any stream capture.  Every call on a device shares the array, so calls whose work overlaps
- * on the GPU (concurrent streams, or host threads) race; serialise them.  Enqueues on `stream`. */
+ * beyond).  The first call on each device, and the first after that device's CUDA context has been
+ * destroyed and recreated (cudaDeviceReset), looks up the array's device address; make that call
+ * before any stream capture begins.  Every call, the first included, enqueues on `stream` a
+ * host-to-device copy of offsets_input (read from the caller's host memory), a clear of the
+ * counters and the render kernels.  Every call on a device shares the array, which keeps the last
+ * call's contents, so calls whose work overlaps on the GPU (concurrent streams, or host threads)
+ * race; serialise them. */
 #define FG_NOALLOC_MAX_INPUT_PIXELS (512u * 512u)
 #define FG_NOALLOC_MAX_SAMPLES 4096u
 FG_API fg_status fg_render_pixelwise_noalloc(const float *d_lambda, const fg_params *params,

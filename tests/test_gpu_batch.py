@@ -62,3 +62,42 @@ def test_batch_autotune_and_tuned_batch(cuda, fgl):
         assert np.array_equal(out.cpu().numpy().view(np.uint32), w.view(np.uint32))
     assert b.tuning.grain_mask_words == best.grain_mask_words
     b.close()
+
+
+def test_batch_of_sweep_images_matches_oracle_tiles(cuda, fgl, orc):
+    """Images of the uneven 64-image sweep (workloads.batched_sweep(64, 7): blob planes of 128^2 to
+    2048^2, radius 0.025-0.2, N 16-256) -- the first of each (size, algorithm) pair, up to ten --
+    rendered together in one batch and checked bit for bit on tiles that the oracle renders exactly
+    (a corner, the centre and the brightest region of each image)."""
+    torch = cuda
+    chosen, seen = [], set()
+    for sp in workloads.batched_sweep(64, seed=7):
+        p = fgl.ParamsBuilder(radius_mean=sp["radius"], n_samples=sp["n"], seed=sp["seed"]).build()
+        d = fgl.derive_common(p, (sp["size"], sp["size"]))
+        algo = fgl.choose_algorithm(p, d)
+        if (sp["size"], algo) in seen:
+            continue
+        seen.add((sp["size"], algo))
+        plane = workloads.blobs_plane(sp["size"], sp["size"], sp["image_seed"])
+        lam = fgl.lambda_plane(fgl.normalize_plane(plane)[0], d.inv_e_pi_r2)
+        chosen.append((sp, p, d, algo, lam))
+    chosen = chosen[:10]
+    assert {c[3] for c in chosen} == {fgl.Algo.Pixel, fgl.Algo.Grain}
+    images = [(torch.from_numpy(lam).cuda(), p, d, algo, lam) for sp, p, d, algo, lam in chosen]
+    b = fgl.Batch(images)
+    b.run()
+    torch.cuda.synchronize()
+    for k, (sp, p, d, algo, lam) in enumerate(chosen):
+        out = b.outputs[k].cpu().numpy()
+        size, t = sp["size"], min(32, sp["size"])
+        op = orc.params_struct("const", sp["radius"], 0.0, 1.0, 0.8, sp["n"], sp["seed"])
+        od, offs, offs_in = orc.derive(op, size, size)
+        iy, ix = np.unravel_index(int(np.argmax(lam)), lam.shape)
+        for x0, y0 in ((0, 0), (size // 2 - t // 2, size // 2 - t // 2), (min(ix, size - t), min(iy, size - t))):
+            name = "pixel" if algo == fgl.Algo.Pixel else "grain"
+            want, _ = orc.render(name, lam, op, od, offs_in if name == "pixel" else offs,
+                                 rect=(x0, y0, x0 + t, y0 + t))
+            got = out[y0:y0 + t, x0:x0 + t]
+            diff = np.count_nonzero(got.view(np.uint32) != want.view(np.uint32))
+            assert diff == 0, f"image {k} ({size}^2 {name}, r {sp['radius']}, N {sp['n']}) tile ({x0},{y0}): {diff} differ"
+    b.close()
