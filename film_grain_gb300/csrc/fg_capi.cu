@@ -542,16 +542,19 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
     const int nplanes = luma ? 1 : 3;
     const size_t n_in = (size_t)cw * ch, n_out = (size_t)d.output_width * d.output_height;
 
-    // host planes, written whole before they are read (no zero fill on the way to the first launch)
-    std::unique_ptr<float[]> planes(new float[3 * n_in]);
-    split_planes(rgb, width, x0, y0, cw, ch, luma ? 1 : 0, planes.get(), planes.get() + n_in,
-                 planes.get() + 2 * n_in);
-    if (cancelled(cancel)) return set_error(FG_ERR_CANCELLED, "cancelled");
-
     keep_pool_memory();
     cudaStream_t s = (cudaStream_t)stream;
     CancelWatch watch(cancel);
-    DevBuf b_lam, b_out, b_rgb8, b_cbcr, b_offs, b_cells, b_diag;
+    DevBuf b_lam, b_out, b_rgb8, b_rgb, b_planes, b_max, b_offs, b_cells, b_diag;
+    // the cropped interleaved RGB to the device, then the colour split, the plane maxima and lambda
+    // there (fg_lambda.cu): no host pass over the image
+    FG_CUDA(b_rgb.alloc(sizeof(float) * 3 * n_in, s), "alloc rgb");
+    FG_CUDA(cudaMemcpy2DAsync(b_rgb.p, sizeof(float) * 3 * (size_t)cw, rgb + 3 * ((size_t)y0 * width + x0),
+                              sizeof(float) * 3 * (size_t)width, sizeof(float) * 3 * (size_t)cw, (size_t)ch,
+                              cudaMemcpyHostToDevice, s),
+            "rgb H2D");
+    FG_CUDA(b_planes.alloc(sizeof(float) * 3 * n_in, s), "alloc planes");
+    FG_CUDA(b_max.alloc(sizeof(unsigned int) * 3, s), "alloc plane maxima");
     FG_CUDA(b_lam.alloc(sizeof(float) * n_in * nplanes, s), "alloc lambda");
     FG_CUDA(b_out.alloc(sizeof(float) * n_out * nplanes, s), "alloc planes");
     FG_CUDA(b_rgb8.alloc(3 * n_out, s), "alloc rgb8");
@@ -567,13 +570,16 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
         FG_CUDA(cudaMemcpyAsync(b_offs.p, tab.data(), tab.size(), cudaMemcpyHostToDevice, s), "offsets H2D");
     }
     float *d_lam = (float *)b_lam.p, *d_out = (float *)b_out.p;
+    st = enqueue_split_lambda((const float *)b_rgb.p, (long long)n_in, luma ? 1 : 0, (float *)b_planes.p,
+                              (unsigned int *)b_max.p, d.inv_e_pi_r2, d_lam, s);
+    if (st != FG_OK) {
+        cudaStreamSynchronize(s);
+        return st;
+    }
     float *d_cb = nullptr, *d_cr = nullptr;
     if (luma) {
-        FG_CUDA(b_cbcr.alloc(sizeof(float) * 2 * n_in, s), "alloc chroma");
-        d_cb = (float *)b_cbcr.p;
+        d_cb = (float *)b_planes.p + n_in;
         d_cr = d_cb + n_in;
-        FG_CUDA(cudaMemcpyAsync(d_cb, planes.get() + n_in, sizeof(float) * 2 * n_in, cudaMemcpyHostToDevice, s),
-                "chroma H2D");
     }
     const size_t mask_bytes = algo == FG_ALGO_GRAIN ? grainwise_mask_bytes(p, d) : 0;
     if (algo == FG_ALGO_PIXEL) {
@@ -583,16 +589,11 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
     } else {
         FG_CUDA(b_cells.alloc(mask_bytes * nplanes, s), "alloc sample masks");
     }
-    std::unique_ptr<float[]> lam(new float[(size_t)n_in * nplanes]);
     for (int c = 0; c < nplanes; c++) {
         if (cancelled(cancel)) {
             cudaStreamSynchronize(s);
             return cancelled_error(watch);
         }
-        float *lc = lam.get() + (size_t)c * n_in;
-        lambda_from_plane(planes.get() + (size_t)c * n_in, (int64_t)n_in, d.inv_e_pi_r2, lc);
-        FG_CUDA(cudaMemcpyAsync(d_lam + (size_t)c * n_in, lc, sizeof(float) * n_in, cudaMemcpyHostToDevice, s),
-                "lambda H2D");
         float *d_plane = d_out + (size_t)c * n_out;
         if (algo == FG_ALGO_PIXEL) {
             EpilogueArgs e;

@@ -11,11 +11,13 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
 #include "../../include/film_grain_gb300.h"
 #include "fg_host.h"
+#include "fg_internal.h"
 #include "fg_rng.cuh"
 
 namespace fg {
@@ -307,6 +309,76 @@ float lambda_from_plane(const float *src, int64_t n, float inv_e_pi_r2, float *d
     return mx;
 }
 
+// ------------------------------------------------------------------ the platform logf, tabulated
+// lambda_plane takes the logarithm of safe = max(1 - c, 1e-6) with c clamped to [0, 1 - 1e-6]
+// (src/model.rs:259-262).  1 - c is always a multiple of 2^-24 in f32, so safe is k * 2^-24 with
+// 17 <= k <= 2^24, or 1e-6 itself when c is NaN: 16,777,201 possible inputs.  The device evaluates
+// RN_f32(log((double)x)), the correctly rounded logarithm unless log(x) lies within a few double ulps
+// of an f32 rounding boundary; the platform logf differs from the correctly rounded value on about
+// 0.1 % of inputs.  Every reachable input where the two differ, or where a last-ulp difference between
+// this host's and the device's double log could move the f32 rounding (|log x| * 2^-50 margin,
+// several double ulps), is recorded with the platform logf's result, so the device reproduces this
+// process's logf bit for bit on every input lambda_plane can produce.
+static uint32_t f32_bits_host(float f) {
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    return b;
+}
+
+// Whether x needs a table entry; *g receives the platform logf.
+static bool logf_exception(float x, float *g) {
+    *g = std::log(x);  // the platform logf, as lambda_value calls it
+    const double d = std::log((double)x);
+    const float f = (float)d;
+    if (d != 0.0) {
+        const double m = std::ldexp(std::fabs(d), -50);
+        if ((float)(d - m) != f || (float)(d + m) != f) return true;
+    }
+    return f32_bits_host(*g) != f32_bits_host(f);
+}
+
+const LogfTable &logf_table() {
+    static LogfTable t;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        t.lo_bits = f32_bits_host(kEps);
+        t.hi_bits = f32_bits_host(1.0f);
+        t.shift = 13;
+        float g;
+        if (logf_exception(kEps, &g)) {  // 1e-6 < 17 * 2^-24: the first key
+            t.keys.push_back(t.lo_bits);
+            t.vals.push_back(f32_bits_host(g));
+        }
+        const int64_t k0 = 17, n = (1 << 24) - k0 + 1;
+        std::vector<std::vector<uint32_t>> part((size_t)chunk_count(n));
+        parallel_chunks(n, [&](int64_t c, int64_t b, int64_t e) {
+            std::vector<uint32_t> &out = part[(size_t)c];
+            for (int64_t i = b; i < e; i++) {
+                const float x = std::ldexp((float)(k0 + i), -24);  // exact
+                float gx;
+                if (logf_exception(x, &gx)) {
+                    out.push_back(f32_bits_host(x));
+                    out.push_back(f32_bits_host(gx));
+                }
+            }
+        });
+        for (const auto &v : part)
+            for (size_t k = 0; k < v.size(); k += 2) {
+                t.keys.push_back(v[k]);
+                t.vals.push_back(v[k + 1]);
+            }
+        const uint32_t nb = ((t.hi_bits - t.lo_bits) >> t.shift) + 1;
+        t.bucket_start.assign((size_t)nb + 1, 0);
+        size_t j = 0;
+        for (uint32_t k = 0; k <= nb; k++) {
+            const uint64_t first = (uint64_t)t.lo_bits + ((uint64_t)k << t.shift);  // first input of bucket k
+            while (j < t.keys.size() && t.keys[j] < first) j++;
+            t.bucket_start[k] = (uint32_t)j;
+        }
+    });
+    return t;
+}
+
 // load_luma_workspace / load_rgb_workspace (src/color.rs:158-213) from interleaved f32 RGB, with the
 // optional ROI crop of apply_roi (src/color.rs:215-231).
 static inline float clamp01(float v) { return clampf(v, 0.0f, 1.0f); }
@@ -333,6 +405,22 @@ void split_planes(const float *rgb, int64_t w, int64_t x0, int64_t y0, int64_t c
 
 }  // namespace fg
 
+// The plane entry points on device memory (src and dst both device pointers): the same passes on the
+// GPU, bit-identical (fg_lambda.cu).  Returns the plane maximum when normalizing; NaN with the error
+// message set when the call fails.
+namespace fg {
+static float device_pass(const float *src, int64_t n, int normalize, int lambda, float inv_e_pi_r2, float *dst) {
+    if (!is_device_ptr(src) || !is_device_ptr(dst)) {
+        set_error(FG_ERR_INVALID, "src and dst must both be host memory or both device memory");
+        return std::nanf("");
+    }
+    float mx = 0.0f;
+    if (device_plane_pass(src, n, normalize, lambda, inv_e_pi_r2, dst, &mx) != FG_OK) return std::nanf("");
+    clear_error();
+    return mx;
+}
+}  // namespace fg
+
 // ------------------------------------------------------------------ C-ABI (host-only entry points)
 extern "C" {
 
@@ -356,16 +444,22 @@ FG_API float fg_default_cell_delta(float radius_mean) { return fg::default_cell_
 
 FG_API float fg_normalize_plane(const float *src, int64_t n, float *dst) {
     if (!src || !dst || n <= 0) return 0.0f;
+    if (fg::is_device_ptr(src) || fg::is_device_ptr(dst)) return fg::device_pass(src, n, 1, 0, 0.0f, dst);
     return fg::normalize_plane(src, n, dst);
 }
 
 FG_API float fg_lambda_from_plane(const float *src, int64_t n, float inv_e_pi_r2, float *dst) {
     if (!src || !dst || n <= 0) return 0.0f;
+    if (fg::is_device_ptr(src) || fg::is_device_ptr(dst)) return fg::device_pass(src, n, 1, 1, inv_e_pi_r2, dst);
     return fg::lambda_from_plane(src, n, inv_e_pi_r2, dst);
 }
 
 FG_API void fg_lambda_plane(const float *normalized, int64_t n, float inv_e_pi_r2, float *dst) {
     if (!normalized || !dst || n <= 0) return;
+    if (fg::is_device_ptr(normalized) || fg::is_device_ptr(dst)) {
+        fg::device_pass(normalized, n, 0, 1, inv_e_pi_r2, dst);
+        return;
+    }
     fg::lambda_plane(normalized, n, inv_e_pi_r2, dst);
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 #include <stdint.h>
 #include <string>
+#include <vector>
 #include "../../include/film_grain_gb300.h"
 
 namespace fg {
@@ -22,5 +23,17 @@ float lambda_from_plane(const float *src, int64_t n, float inv_e_pi_r2, float *d
 void split_planes(const float *rgb, int64_t w, int64_t x0, int64_t y0, int64_t cw, int64_t ch, int luma, float *p0,
                   float *p1, float *p2);
 void fill_stats(const fg_params &p, const fg_derived &d, int32_t algo, fg_render_stats *s);
+
+// The platform logf (what the crate's f32::ln calls in lambda_plane) on every input lambda_plane can
+// produce, as the inputs where it differs from RN_f32(log((double)x)): sorted keys (input bit
+// patterns) with their logf bit patterns, bucketed by (bits - lo_bits) >> shift.  Built once per
+// process from this process's own logf (16.8 million evaluations spread over the host cores).
+struct LogfTable {
+    uint32_t lo_bits, hi_bits;           // the domain [1e-6f, 1.0f] as f32 bit patterns
+    int shift;
+    std::vector<uint32_t> bucket_start;  // ((hi_bits - lo_bits) >> shift) + 2 entries
+    std::vector<uint32_t> keys, vals;
+};
+const LogfTable &logf_table();
 
 }  // namespace fg

@@ -36,4 +36,15 @@ fg_status enqueue_grainwise(const GrainwiseArgs &a, cudaStream_t s);
 fg_status enqueue_grainwise_epilogue(const GrainwiseArgs &a, float *d_out, int mode, unsigned char *d_rgb8,
                                      const float *d_cb, const float *d_cr, cudaStream_t s);
 
+// Device prelude of the whole-image render (fg_lambda.cu): the colour split of the cropped interleaved
+// RGB (n_in pixels) into d_planes (3 x n_in: Y, Cb, Cr or R, G, B), the plane maxima (d_max: 3 words)
+// and lambda of the rendered planes (1 or 3) into d_lam.
+fg_status enqueue_split_lambda(const float *d_rgb, long long n_in, int luma, float *d_planes, unsigned int *d_max,
+                               float inv_e_pi_r2, float *d_lam, cudaStream_t s);
+// normalize_plane (normalize), lambda_plane (lambda) or both on device memory; max_out receives the
+// plane maximum when normalizing.
+fg_status device_plane_pass(const float *src, int64_t n, int normalize, int lambda, float inv_e_pi_r2, float *dst,
+                            float *max_out);
+fg_status device_logf_table(LogfTableDev *out);
+
 }  // namespace fg

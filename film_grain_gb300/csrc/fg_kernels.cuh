@@ -126,6 +126,13 @@ struct EpilogueArgs {
     const float *p0, *p1;       // rgb: rendered channels 0 and 1 (values)
 };
 
+// The platform-logf table on the device (fg_lambda.cu platform_logf).
+struct LogfTableDev {
+    const uint32_t *bucket_start, *keys, *vals;
+    uint32_t lo_bits, hi_bits;
+    int shift;
+};
+
 cudaError_t launch_cell_params(const float *lam, int in_w, int in_h, float delta, CellParam *cells, cudaStream_t s);
 // defer: null (fat CTAs over every block) or a buffer of 2 + nbx*nby ints (lean pass, then fat CTAs
 // over the deferred blocks).

@@ -382,7 +382,10 @@ FG_HD double normal_sample(double mean, double sd, Rng &rng) {
 // ------------------------------------------------------------------ exp(t) rounded to f32
 // LogNormal::sample(...) as f32 (src/model.rs:141-142) is RN_f32(exp(t)) of an f64 exp.  FP64
 // throughput is a small fraction of FP32 on this part, so exp(t) is evaluated in double-float
-// arithmetic on the FP32 pipes:
+// arithmetic on the FP32 pipes, by a table-driven method in the manner of P. T. P. Tang ("Table-driven
+// implementation of the exponential function in IEEE floating-point arithmetic", ACM TOMS 15(2),
+// 1989): a Cody-Waite reduction by ln 2 split into three parts, a second reduction against a table of
+// exp(j/64), and a short polynomial:
 //   t = th + tm + tt exactly (three floats cut from t's 53-bit significand);
 //   r = t - k*ln2 with ln2 = L1 + L2 + L3 (L1 has 12 significant bits, so k*L1 is exact);
 //   exp(r) = T[j] * exp(s), s = r - j/64, T[j] = exp(j/64) as a float pair (exp_table.h);

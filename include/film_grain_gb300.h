@@ -132,16 +132,21 @@ FG_API int32_t fg_choose_algorithm(const fg_params *params, const fg_derived *de
 /* default_cell_delta (src/params.rs:255-261). */
 FG_API float fg_default_cell_delta(float radius_mean);
 
-/* normalize_plane (src/model.rs:228-250); returns the plane maximum.  Host buffers. */
+/* normalize_plane (src/model.rs:228-250); returns the plane maximum.  src and dst are both host
+ * memory (a pass over the host cores) or both device memory (a synchronous pass on the GPU, same bits;
+ * NaN is returned, with the message set, if it fails). */
 FG_API float fg_normalize_plane(const float *src, int64_t n, float *dst);
 
-/* lambda_plane (src/model.rs:252-265).  Host buffers (the crate computes lambda on the host with
- * the platform logf; so does this library, to stay bit-identical). */
+/* lambda_plane (src/model.rs:252-265).  Host or device buffers as for fg_normalize_plane.  The crate
+ * takes the logarithm with f32::ln, the platform logf; the device pass reproduces this process's logf
+ * bit for bit (a table of the inputs where it differs from the correctly rounded logarithm, built once
+ * per process from logf itself). */
 FG_API void fg_lambda_plane(const float *normalized, int64_t n, float inv_e_pi_r2, float *dst);
 
 /* lambda_plane(normalize_plane(src)) in one pass (the same per-element operations, so the same bits),
  * without the normalised plane in memory; returns the plane maximum as fg_normalize_plane does.  The
- * crate runs the two steps in turn (src/lib.rs:140-166 via src/model.rs:228-265).  Host buffers. */
+ * crate runs the two steps in turn (src/lib.rs:140-166 via src/model.rs:228-265).  Host or device
+ * buffers as for fg_normalize_plane. */
 FG_API float fg_lambda_from_plane(const float *src, int64_t n, float inv_e_pi_r2, float *dst);
 
 /* ---------------------------------------------------------------------------------------------
@@ -197,7 +202,8 @@ FG_API fg_status fg_render_pixelwise_noalloc(const float *d_lambda, const fg_par
  * params' ROI, when set, is cropped first (apply_roi, src/color.rs:215-231).
  * out_rgb8: output_height x output_width x 3 u8 (host memory), sized from fg_dry_run or fg_derive.
  * Luma mode renders Y only and recombines it with nearest-resized Cb/Cr; RGB mode renders the three
- * planes with the same seed.  The colour recombination and u8 packing run fused on the GPU. */
+ * planes with the same seed.  Only the cropped RGB goes to the GPU: the colour split, normalize_plane,
+ * lambda_plane, the integrators, the colour recombination and the u8 packing all run there. */
 FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height, const fg_params *params,
                                  uint8_t *out_rgb8, fg_render_stats *stats, const volatile int32_t *cancel,
                                  void *stream);

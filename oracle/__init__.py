@@ -90,6 +90,7 @@ def lib():
             "orc_normal_draws": (None, [ctypes.c_double, ctypes.c_double, u64, i64, f64p]),
             "orc_uniform_f32_draws": (None, [f32, f32, u64, i64, f32p]),
             "orc_log_gamma": (ctypes.c_double, [ctypes.c_double]),
+            "orc_libm_f64": (None, [i32, ctypes.c_void_p, i64, ctypes.c_void_p]),
             "orc_threads": (i32, []),
             "orc_grain_total": (u64, [f32p, P(OParams), P(ODerived), i64, i64, i32]),
             "orc_grainwise_rows": (ctypes.c_int, [f32p, P(OParams), P(ODerived), f32p, i64, i64, u64p, i32, u64p,
@@ -314,6 +315,14 @@ def uniform_f32_draws(low: float, high: float, seed_u64: int, n: int) -> np.ndar
 
 def log_gamma(x: float) -> float:
     return lib().orc_log_gamma(x)
+
+
+def libm_f64(name: str, x: np.ndarray) -> np.ndarray:
+    """The platform libm's exp / log / tan on f64 values (the crate's samplers call these)."""
+    src = np.ascontiguousarray(x, np.float64)
+    out = np.empty_like(src)
+    lib().orc_libm_f64({"exp": 0, "log": 1, "tan": 2}[name], src.ctypes.data, src.size, out.ctypes.data)
+    return out
 
 
 def threads() -> int:

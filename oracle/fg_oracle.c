@@ -795,6 +795,11 @@ ORC_EXPORT void orc_uniform_f32_draws(float low, float high, uint64_t seed_u64, 
     for (int64_t i = 0; i < n; i++) out[i] = o_uniform_sample(&u, &r);
 }
 ORC_EXPORT double orc_log_gamma(double x) { return o_log_gamma(x); }
+/* The platform libm's f64 exp / log / tan (what the crate's samplers call) over an array: which = 0 exp,
+ * 1 log, 2 tan. */
+ORC_EXPORT void orc_libm_f64(int32_t which, const double *x, int64_t n, double *out) {
+    for (int64_t i = 0; i < n; i++) out[i] = which == 0 ? exp(x[i]) : (which == 1 ? log(x[i]) : tan(x[i]));
+}
 ORC_EXPORT int32_t orc_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();
