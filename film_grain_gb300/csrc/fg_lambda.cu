@@ -24,8 +24,11 @@ namespace fg {
 constexpr float kLamEps = 1e-6f;    // src/model.rs:10
 constexpr float kMaxLambda = 1.0e6f;  // src/model.rs:11
 
-__device__ __forceinline__ float clampf_d(float x, float lo, float hi) {  // f32::clamp: NaN passes
-    if (x < lo) x = lo;
+// f32::clamp: a NaN passes through with its bits (tested on the integer bits, so that no NaN-propagating
+// min/max can replace its payload with the canonical NaN).
+__device__ __forceinline__ float clampf_d(float x, float lo, float hi) {
+    if ((__float_as_uint(x) & 0x7fffffffu) > 0x7f800000u) return x;
+    if (x < lo) x = lo;  // comparisons, not min/max: -0.0 stays -0.0 as in f32::clamp
     if (x > hi) x = hi;
     return x;
 }

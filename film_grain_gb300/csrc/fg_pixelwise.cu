@@ -30,6 +30,7 @@
 #include "fg_rng.cuh"
 #include "fg_color.cuh"
 #include "fg_pixelwise.cuh"
+#include "fg_pixelwise_sparse.cuh"
 
 namespace fg {
 
@@ -77,6 +78,42 @@ __global__ void __launch_bounds__(C::kThreads, C::kCtasPerSm)
     const bool deferred = pixelwise_block<C>(a, a.bx0 + (int)(blockIdx.x % (unsigned)a.nbx),
                                              a.by0 + (int)(blockIdx.x / (unsigned)a.nbx), smem_raw, list != nullptr);
     if (deferred && threadIdx.x == 0) list[1 + atomicAdd(list, 1)] = id;
+}
+
+// The sparse pass: one CTA per sparse block (grid row-major from (sbx0, sby0)); the fat-grid blocks of
+// a block it leaves are appended to the list (list[0] = count, list[1..] = fat-grid block indices).
+__global__ void __launch_bounds__(PwSparse::kThreads, PwSparse::kCtasPerSm)
+    pixelwise_sparse_kernel(const __grid_constant__ PixelwiseArgs a, const PwSparseGrid g, int nby,
+                            int *__restrict__ list) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int sbx = g.sbx0 + (int)(blockIdx.x % (unsigned)g.nsbx), sby = g.sby0 + (int)(blockIdx.x / (unsigned)g.nsbx);
+    const bool deferred = pixelwise_sparse_block(a, g, sbx, sby, smem_raw);
+    if (deferred && threadIdx.x == 0) sparse_defer(a, g, sbx, sby, nby, list);
+}
+
+static int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+
+// The sparse pass's block grid: the largest edge of 4, 2 or 1 fat-grid blocks whose window fits its
+// bitmask and whose grid still gives every CTA slot several blocks; false when no edge fits (or N is
+// above one offset chunk), and the plane takes the lean pass instead.
+static bool plan_sparse(const PixelwiseArgs &a, int nby, int sms, PwSparseGrid *g) {
+    if (a.n > kPwKChunk || !(a.rm >= 0.0f)) return false;
+    for (int R = 4; R >= 1; R >>= 1) {
+        const float bs = a.bsize * (float)R;
+        const double edge = std::floor(((double)bs + 2.0 * a.rm) / a.delta) + 3.0;
+        const double wpr = std::ceil(edge / 32.0);
+        if (edge > PwSparse::kRowsMax || wpr * edge > PwSparse::kMaskWords) continue;
+        const int sbx0 = floor_div(a.bx0, R), sbx1 = floor_div(a.bx0 + a.nbx - 1, R);
+        const int sby0 = floor_div(a.by0, R), sby1 = floor_div(a.by0 + nby - 1, R);
+        const long long blocks = (long long)(sbx1 - sbx0 + 1) * (sby1 - sby0 + 1);
+        if (R > 1 && blocks < 4LL * sms * PwSparse::kCtasPerSm) continue;
+        g->bs = bs;
+        g->ratio = R;
+        g->sbx0 = sbx0; g->sby0 = sby0;
+        g->nsbx = sbx1 - sbx0 + 1; g->nsby = sby1 - sby0 + 1;
+        return true;
+    }
+    return false;
 }
 
 // The root blocks the lean pass deferred, in fat CTAs: persistent, each CTA taking the next listed
@@ -156,12 +193,21 @@ cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, cudaSt
     }
     e = cudaMemsetAsync(defer, 0, 2 * sizeof(int), s);  // [0] the fat pass's counter, [1] the list's count
     if (e != cudaSuccess) return e;
-    pixelwise_kernel<PwLean><<<(unsigned)nblocks, PwLean::kThreads, lean_smem, s>>>(a, defer + 1);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
     int dev = 0, sms = 0;
     e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    PwSparseGrid g;
+    if (plan_sparse(a, nby, sms, &g)) {
+        const size_t sparse_smem = sizeof(PwSparseShared);
+        e = set_smem(pixelwise_sparse_kernel, sparse_smem);
+        if (e != cudaSuccess) return e;
+        pixelwise_sparse_kernel<<<(unsigned)((long long)g.nsbx * g.nsby), PwSparse::kThreads, sparse_smem, s>>>(
+            a, g, nby, defer + 1);
+    } else {
+        pixelwise_kernel<PwLean><<<(unsigned)nblocks, PwLean::kThreads, lean_smem, s>>>(a, defer + 1);
+    }
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const long long grid = std::min<long long>(nblocks, (long long)std::max(1, sms) * PwFat::kCtasPerSm);
     pixelwise_deferred_kernel<<<(unsigned)grid, PwFat::kThreads, fat_smem, s>>>(a, defer + 1);

@@ -45,7 +45,8 @@ def test_device_normalize_and_lambda_from_plane(cuda, fgl):
     planes = [workloads.blobs_plane(320, 200, 2),                                  # already in [0, 1]
               (rng.random((256, 256)) * 3.7).astype(np.float32),                    # normalised by its max
               np.where(rng.random((64, 96)) < 0.01, np.nan, rng.random((64, 96))).astype(np.float32),
-              np.full((17, 13), 0.25, np.float32)]
+              np.full((17, 13), 0.25, np.float32),
+              np.array([[-0.0, 0.0, np.nan, -np.nan, 0.5], [1.0, -1.0, np.inf, -np.inf, 0.25]], np.float32)]
     for plane in planes:
         for fn, args in (("fg_normalize_plane", ()), ("fg_lambda_from_plane", (ctypes.c_float(21.5),))):
             host, dev, mh, md = _host_and_device(fgl, torch, fn, plane, *args)
