@@ -241,9 +241,18 @@ fg_status enqueue_pixelwise(const float *d_lam, const fg_params &p, const fg_der
     FG_CUDA(cudaMemsetAsync(d_out, 0, sizeof(float) * (size_t)out_w * out_h, s), "memset");
     PixelwiseArgs a = pixelwise_args(p, d, pl, d_lam, d_cells, d_offs_in, d_out, d_diag);
     a.cancel = d_cancel;
-    DevBuf defer;  // the lean pass's list of deferred root blocks (none without allocation: fat CTAs only)
-    if (may_allocate) FG_CUDA(defer.alloc((2 + (size_t)pl.nbx * pl.nby) * sizeof(int), s), "alloc defer list");
-    FG_CUDA(launch_pixelwise(a, pl.nby, static_cast<int *>(defer.p), s), "pixelwise kernel");
+    DevBuf defer;  // the first pass's list of deferred root blocks (none without allocation: fat CTAs only)
+    DevBuf cellmask;  // the sparse pass's emptiness bitmask of the plane's cells
+    if (may_allocate) {
+        FG_CUDA(defer.alloc((2 + (size_t)pl.nbx * pl.nby) * sizeof(int), s), "alloc defer list");
+        const size_t mask_bytes = pixelwise_cellmask_bytes(a, pl.nby);
+        if (mask_bytes && cellmask.alloc(mask_bytes, s) != cudaSuccess) {
+            cudaGetLastError();  // no room for the bitmask: the plane takes the lean pass
+            cellmask.p = nullptr;
+        }
+    }
+    FG_CUDA(launch_pixelwise(a, pl.nby, static_cast<int *>(defer.p), static_cast<unsigned int *>(cellmask.p), s),
+            "pixelwise kernel");
     EpilogueArgs e;
     if (colour) e = *colour;
     else std::memset(&e, 0, sizeof e);

@@ -136,7 +136,11 @@ struct LogfTableDev {
 cudaError_t launch_cell_params(const float *lam, int in_w, int in_h, float delta, CellParam *cells, cudaStream_t s);
 // defer: null (fat CTAs over every block) or a buffer of 2 + nbx*nby ints (lean pass, then fat CTAs
 // over the deferred blocks).
-cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, cudaStream_t s);
+// cellmask: null, or pixelwise_cellmask_bytes(a, nby) bytes for the sparse pass's plane bitmask (the
+// plane then takes the sparse pass, else the lean pass).
+cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, unsigned int *cellmask, cudaStream_t s);
+// Scratch bytes of the sparse pass's plane bitmask for this plane; 0 when the plane does not take it.
+size_t pixelwise_cellmask_bytes(const PixelwiseArgs &a, int nby);
 // Whether a plane runs on the per-sample kernel instead of the block kernel, and its launch.
 bool pixelwise_prefers_regen(const PixelwiseArgs &a);
 cudaError_t launch_pixelwise_regen(const PixelwiseArgs &a, cudaStream_t s);

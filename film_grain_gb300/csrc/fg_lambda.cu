@@ -7,6 +7,7 @@
 // could under a last-ulp difference of the double log), by the platform logf's own result, so the
 // device plane equals the host plane on every input.  Everything else is exact f32 arithmetic in the
 // host code's order (--fmad=false, explicit round-to-nearest operations).
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -31,6 +32,15 @@ __device__ __forceinline__ float clampf_d(float x, float lo, float hi) {
     if (x < lo) x = lo;  // comparisons, not min/max: -0.0 stays -0.0 as in f32::clamp
     if (x > hi) x = hi;
     return x;
+}
+
+// v / den as the host's f32 division gives it, NaN bits included: a NaN dividend comes back unchanged
+// (x86 and Arm propagate the dividend's payload; CUDA's division returns its canonical NaN), and a NaN
+// made by the division itself (inf / inf) is the host's default NaN, `host_nan`.
+__device__ __forceinline__ float div_like_host(float v, float den, uint32_t host_nan) {
+    if ((__float_as_uint(v) & 0x7fffffffu) > 0x7f800000u) return v;
+    const float q = FG_FDIV(v, den);
+    return (__float_as_uint(q) & 0x7fffffffu) > 0x7f800000u ? __uint_as_float(host_nan) : q;
 }
 
 // The platform logf on [1e-6, 1].
@@ -111,7 +121,8 @@ __global__ void plane_max_kernel(const float *__restrict__ src, long long n, uns
 // (src/model.rs:255-263): plane c of `src` (n elements each) -> plane c of `dst`.
 __global__ void normalize_lambda_kernel(const float *__restrict__ src, long long n, int nplanes,
                                         const unsigned int *__restrict__ maxbits, int normalize, int lambda,
-                                        float inv_e_pi_r2, LogfTableDev t, float *__restrict__ dst) {
+                                        float inv_e_pi_r2, LogfTableDev t, uint32_t host_nan,
+                                        float *__restrict__ dst) {
     const long long total = n * nplanes;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (long long)gridDim.x * blockDim.x) {
@@ -122,7 +133,7 @@ __global__ void normalize_lambda_kernel(const float *__restrict__ src, long long
             const bool already = mx <= FG_FADD(1.0f, kLamEps);
             float den = FG_FADD(mx, kLamEps);
             if (den < kLamEps) den = kLamEps;
-            v = clampf_d(already ? v : FG_FDIV(v, den), 0.0f, 1.0f - kLamEps);
+            v = clampf_d(already ? v : div_like_host(v, den, host_nan), 0.0f, 1.0f - kLamEps);
         }
         if (lambda) {
             const float cl = clampf_d(v, 0.0f, 1.0f - kLamEps);
@@ -176,6 +187,16 @@ fg_status device_logf_table(LogfTableDev *out) {
     return FG_OK;
 }
 
+// The NaN this host's f32 division makes from inf / inf (x86: the negative quiet NaN, Arm: the positive
+// one), computed at run time on the host itself.
+static uint32_t host_default_nan() {
+    volatile float inf = INFINITY;
+    const float q = inf / inf;
+    uint32_t b;
+    std::memcpy(&b, &q, 4);
+    return b;
+}
+
 static unsigned grid_for(long long n) {
     long long g = (n + 255) / 256;
     return (unsigned)std::max<long long>(1, std::min<long long>(g, 152LL * 16));
@@ -192,7 +213,7 @@ fg_status enqueue_split_lambda(const float *d_rgb, long long n_in, int luma, flo
                                                       d_max);
     const int nplanes = luma ? 1 : 3;
     normalize_lambda_kernel<<<grid_for(n_in * nplanes), 256, 0, s>>>(d_planes, n_in, nplanes, d_max, 1, 1, inv_e_pi_r2,
-                                                                     t, d_lam);
+                                                                     t, host_default_nan(), d_lam);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "lambda kernels");
     return FG_OK;
@@ -216,7 +237,8 @@ fg_status device_plane_pass(const float *src, int64_t n, int normalize, int lamb
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
-        normalize_lambda_kernel<<<grid_for(n), 256>>>(src, n, 1, d_max, normalize, lambda, inv_e_pi_r2, t, dst);
+        normalize_lambda_kernel<<<grid_for(n), 256>>>(src, n, 1, d_max, normalize, lambda, inv_e_pi_r2, t,
+                                                      host_default_nan(), dst);
         e = cudaGetLastError();
     }
     unsigned int mb = 0;

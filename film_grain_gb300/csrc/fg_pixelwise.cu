@@ -80,18 +80,32 @@ __global__ void __launch_bounds__(C::kThreads, C::kCtasPerSm)
     if (deferred && threadIdx.x == 0) list[1 + atomicAdd(list, 1)] = id;
 }
 
-// The sparse pass: one CTA per sparse block (grid row-major from (sbx0, sby0)); the fat-grid blocks of
-// a block it leaves are appended to the list (list[0] = count, list[1..] = fat-grid block indices).
+// The sparse pass: one CTA per sparse block (grid row-major from (sbx0, sby0)); the fat-grid blocks it
+// leaves are appended to the list (list[0] = count, list[1..] = fat-grid block indices).
 __global__ void __launch_bounds__(PwSparse::kThreads, PwSparse::kCtasPerSm)
     pixelwise_sparse_kernel(const __grid_constant__ PixelwiseArgs a, const PwSparseGrid g, int nby,
                             int *__restrict__ list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int sbx = g.sbx0 + (int)(blockIdx.x % (unsigned)g.nsbx), sby = g.sby0 + (int)(blockIdx.x / (unsigned)g.nsbx);
-    const bool deferred = pixelwise_sparse_block(a, g, sbx, sby, smem_raw);
-    if (deferred && threadIdx.x == 0) sparse_defer(a, g, sbx, sby, nby, list);
+    pixelwise_sparse_root(a, g, sbx, sby, nby, list, smem_raw);
+}
+
+// The plane's emptiness bitmask (pixelwise_sparse_block step 0): one thread per mask word.
+__global__ void __launch_bounds__(256) cell_mask_kernel(const __grid_constant__ PixelwiseArgs a, const PwSparseGrid g,
+                                                        unsigned int *__restrict__ cellmask) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.gw * g.ghw) return;
+    cell_mask_word(a, g, t, cellmask);
 }
 
 static int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+
+// The window bounds of pixelwise_sparse_block, by the same f32 operations.
+static int window_lo(float X0, const PixelwiseArgs &a) { return (int)std::floor((X0 - a.rm) / a.delta); }
+static int window_hi(float X1, const PixelwiseArgs &a) { return (int)std::floor((X1 + a.rm) / a.delta); }
+
+// Largest plane bitmask the sparse pass allocates (larger planes take the lean pass).
+constexpr double kCellMaskMaxBytes = 16.0 * (1ull << 30);
 
 // The sparse pass's block grid: the largest edge of 4, 2 or 1 fat-grid blocks whose window fits its
 // bitmask and whose grid still gives every CTA slot several blocks; false when no edge fits (or N is
@@ -111,9 +125,35 @@ static bool plan_sparse(const PixelwiseArgs &a, int nby, int sms, PwSparseGrid *
         g->ratio = R;
         g->sbx0 = sbx0; g->sby0 = sby0;
         g->nsbx = sbx1 - sbx0 + 1; g->nsby = sby1 - sby0 + 1;
-        return true;
+        // the bitmask covers every block's window with a two-cell margin
+        const int gi0 = window_lo((float)sbx0 * bs, a) - 2, gi1 = window_hi((float)(sbx1 + 1) * bs, a) + 2;
+        const int gj0 = window_lo((float)sby0 * bs, a) - 2, gj1 = window_hi((float)(sby1 + 1) * bs, a) + 2;
+        g->cellmask = nullptr;
+        g->gi0 = gi0;
+        g->gj0 = gj0;
+        g->gw = gi1 - gi0 + 1;
+        g->ghw = (gj1 - gj0 + 1 + 31) / 32 + 1;  // one more word row for the windows' shifted reads
+        return (double)g->gw * g->ghw * 4.0 <= kCellMaskMaxBytes;
     }
     return false;
+}
+
+static int sm_count() {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                    cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return sms;
+}
+
+size_t pixelwise_cellmask_bytes(const PixelwiseArgs &a, int nby) {
+    if (pixelwise_prefers_regen(a)) return 0;
+    PwSparseGrid g;
+    const int sms = sm_count();
+    if (sms <= 0 || !plan_sparse(a, nby, sms, &g)) return 0;
+    return (size_t)g.gw * g.ghw * sizeof(unsigned int);
 }
 
 // The root blocks the lean pass deferred, in fat CTAs: persistent, each CTA taking the next listed
@@ -178,7 +218,7 @@ static cudaError_t set_smem(K k, size_t smem) {
     return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, cudaStream_t s) {
+cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, unsigned int *cellmask, cudaStream_t s) {
     if (pixelwise_prefers_regen(a)) return launch_pixelwise_regen(a, s);
     const size_t lean_smem = sizeof(PwShared<PwLean>), fat_smem = sizeof(PwShared<PwFat>);
     cudaError_t e = set_smem(pixelwise_kernel<PwLean>, lean_smem);
@@ -198,7 +238,10 @@ cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, cudaSt
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     PwSparseGrid g;
-    if (plan_sparse(a, nby, sms, &g)) {
+    if (cellmask && plan_sparse(a, nby, sms, &g)) {
+        g.cellmask = cellmask;
+        const long long words = (long long)g.gw * g.ghw;
+        cell_mask_kernel<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(a, g, cellmask);
         const size_t sparse_smem = sizeof(PwSparseShared);
         e = set_smem(pixelwise_sparse_kernel, sparse_smem);
         if (e != cudaSuccess) return e;

@@ -6,17 +6,19 @@
 // A CTA owns a square block of input space [X0, X1) x [Y0, Y1) (edge a power of two, `ratio` fat-grid
 // blocks per side) and evaluates every sample (pixel, offset) whose point xg = ((x + 0.5) * inv_zoom) -
 // offsets_input[k] lands in it:
-//   1. the emptiness of every cell of the window that the owned samples can reach becomes one bit of
-//      a row-major bitmask: each lane owns one of 32 consecutive columns (its column stage of the cell
-//      hash computed once per run of rows), and per row the warp's ballot is one mask word; a cell is
-//      empty when its first uniform does not exceed its Knuth threshold (cell_count_h);
-//   2. the set bits, ranked in row-major order, list the non-empty cells; their grain counts (the
+//   0. (cell_mask_kernel, before the pass) the emptiness of every cell of the plane's cell grid is one
+//      bit of a column-major bitmask in global memory: a thread owns one column and 32 rows (the column
+//      stage of the cell hash computed once) and stores one word; a cell is empty when its first
+//      uniform does not exceed its Knuth threshold (cell_count_h).  Every cell is hashed once per plane;
+//   1. the CTA copies the bits of its window -- the cells its owned samples can reach -- into shared
+//      memory (column-major: word k of window column c holds rows 32k .. 32k + 31);
+//   2. the set bits, ranked in column-major order, list the non-empty cells; their grain counts (the
 //      Poisson draws of src/pixelwise.rs:77-82) are prefix-summed into a CSR over the list and their
 //      grains (centre, radius^2) regenerated into shared memory;
 //   3. each thread takes the owned pixels of one offset (or a share of them) and runs the reference's
-//      per-sample test: for each cell row j0..j1 of the sample's range (src/pixelwise.rs:55-58), the
-//      bits of columns i0..i1 are cut from the mask, and when any is set their grains -- contiguous in
-//      the CSR, since cells of one row follow each other in the list -- get the disk test
+//      per-sample test: for each cell column i0..i1 of the sample's range (src/pixelwise.rs:55-58), the
+//      bits of rows j0..j1 are cut from the mask, and when any is set their grains -- contiguous in
+//      the CSR, since cells of one column follow each other in the list -- get the disk test
 //      dx*dx + dy*dy <= r*r (src/pixelwise.rs:96-99);
 //   4. hit counts go to per-pixel shared counters, then to the output plane (integers, exact in f32).
 // The indicator is an OR over the grains of the sample's cells, so the result equals the reference's
@@ -32,30 +34,61 @@ struct PwSparse {
     static constexpr int kListMax = 2048;    // non-empty cells of the window
     static constexpr int kMaskWords = 1024;  // window bitmask (32768 cells)
     static constexpr int kRowsMax = 256;     // window rows
-    static constexpr int kRowBand = 8;       // rows one warp hashes per work unit
 };
 
 struct PwSparseShared {
     float4 grains[PwSparse::kGrainMax];
-    unsigned int mask[PwSparse::kMaskWords];
-    unsigned short wrank[PwSparse::kMaskWords];  // non-empty cells before each mask word (row-major)
-    unsigned short list[PwSparse::kListMax];     // non-empty cells: window index j * Wc + i, row-major
+    uint2 mask2[PwSparse::kMaskWords];           // (word w, the next word of the same column or 0)
+    unsigned short wrank[PwSparse::kMaskWords];  // non-empty cells before each mask word (column-major)
+    unsigned short list[PwSparse::kListMax];     // non-empty cells: window index i * Hc + j, column-major
     unsigned short gstart[PwSparse::kListMax + 1];
     int4 rect[kPwKChunk];                       // owned pixel rectangle per offset: xa, xe, ya, ye
     unsigned int cnt[kPwFootMax];
     int wsum[40];
-    int fx0, fx1, fy0, fy1, nsamples;
+    int wi0, wi1, wj0, wj1, Wc, Hc, hw;         // the window: cells [wi0, wi1] x [wj0, wj1], hw words per column
+    int fx0, fx1, fy0, fy1, nsamples;           // owned-pixel footprint, owned samples
+    int rw_min, rw_max, rh_min, rh_max;         // extremes of the offsets' rectangle widths and heights
     int stop;
     float est_grains, est_cells;
 };
 
 // Geometry of the sparse pass: block edge `bs` (input pixels) = ratio x the fat grid's edge, block grid
-// origin and width; the fat grid is (a.bx0, a.by0, a.nbx) with a.bsize.
+// origin and width (the fat grid is (a.bx0, a.by0, a.nbx) with a.bsize); and the plane's emptiness
+// bitmask: cells [gi0, gi0 + gw) x [gj0, gj0 + 32 ghw), word (c, k) = cellmask[k * gw + c] holding rows
+// gj0 + 32k .. + 31 of column gi0 + c (bit r = row gj0 + 32k + r).
 struct PwSparseGrid {
     float bs;
     int ratio;
     int sbx0, sby0, nsbx, nsby;
+    const unsigned int *cellmask;
+    int gi0, gj0, gw, ghw;
 };
+
+// The plane's emptiness bitmask (step 0): thread t = (word row k = t / gw, column c = t % gw).
+__device__ __forceinline__ void cell_mask_word(const PixelwiseArgs &a, const PwSparseGrid &g, long long t,
+                                               unsigned int *cellmask) {
+    const int c = (int)(t % g.gw), k = (int)(t / g.gw);
+    const int i = g.gi0 + c;
+    const uint64_t colh = cell_col_hash(a.seed, i);
+    long long ix = (long long)floorf(FG_FMUL((float)i, a.delta));
+    ix = ix < 0 ? 0 : (ix > a.in_w - 1 ? a.in_w - 1 : ix);
+    int iy_prev = -1;
+    long long thresh = 0;
+    unsigned int word = 0;
+#pragma unroll 4
+    for (int r = 0; r < 32; r++) {
+        const int j = g.gj0 + 32 * k + r;
+        long long iy = (long long)floorf(FG_FMUL((float)j, a.delta));
+        iy = iy < 0 ? 0 : (iy > a.in_h - 1 ? a.in_h - 1 : iy);
+        if ((int)iy != iy_prev) {
+            iy_prev = (int)iy;
+            thresh = a.cells[iy * a.in_w + ix].thresh;
+        }
+        const long long v = (long long)(small_first_u64(cell_row_hash(colh, j)) >> 11);
+        word |= (v > thresh ? 1u : 0u) << r;
+    }
+    cellmask[t] = word;
+}
 
 // The reference's per-sample loop for a sample the staged window cannot serve (out of line: rare).
 __device__ __noinline__ bool sparse_regen_sample(const PixelwiseArgs &a, float xg, float yg, int i0, int i1, int j0,
@@ -87,19 +120,191 @@ __device__ __forceinline__ void sparse_defer(const PixelwiseArgs &a, const PwSpa
     }
 }
 
-// One sparse block (all threads of the CTA; `smem_raw` holds PwSparseShared).  Returns true when the
-// block was left to the fat pass (nothing rendered).
-__device__ __forceinline__ bool pixelwise_sparse_block(const PixelwiseArgs &a, const PwSparseGrid &g, int sbx,
-                                                       int sby, unsigned char *smem_raw) {
+// Whether sample (xg, yg) is covered: the reference's cell range (src/pixelwise.rs:55-58), one
+// 64-bit shared load per cell column for the bits of rows j0..j1, the disk test on the grains of the
+// set bits (src/pixelwise.rs:96-99); samples whose range leaves the window take the per-sample loop.
+__device__ __forceinline__ bool sparse_sample_hit(const PixelwiseArgs &a, const PwSparseShared &S, float xg, float yg,
+                                                  int j0, int j1, unsigned long long &slow) {
+    if (!(a.rm > 0.0f)) return false;
+    const int i0 = f2i_floor(FG_FDIV(FG_FSUB(xg, a.rm), a.delta));
+    const int i1 = f2i_floor(FG_FDIV(FG_FADD(xg, a.rm), a.delta));
+    if (i0 > i1 || j0 > j1) return false;  // no cell (src/pixelwise.rs:60-62)
+    const int wi0 = S.wi0, wj0 = S.wj0, hw = S.hw;
+    const unsigned span = (unsigned)(j1 - j0);
+    if (i0 < wi0 || i1 > S.wi1 || j0 < wj0 || j1 > S.wj1 || span >= 32u) {
+        slow++;
+        return sparse_regen_sample(a, xg, yg, i0, i1, j0, j1);
+    }
+    const int r0 = j0 - wj0, b0 = r0 & 31;
+    const unsigned keep = (2u << span) - 1u;  // span <= 31: 2u << 31 wraps to 0 and keep is all ones
+    const unsigned below = (1u << b0) - 1u;
+    int w = (i0 - wi0) * hw + (r0 >> 5);
+    for (int i = i0; i <= i1; i++, w += hw) {
+        const uint2 m = S.mask2[w];
+        const unsigned bits = __funnelshift_r(m.x, m.y, b0) & keep;
+        if (!bits) continue;
+        const int rank = S.wrank[w] + __popc(m.x & below);
+        const int ge = S.gstart[rank + __popc(bits)];
+        for (int g = S.gstart[rank]; g < ge; g++) {
+            const float4 G = S.grains[g];
+            const float dx = FG_FSUB(xg, G.x), dy = FG_FSUB(yg, G.y);
+            if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= G.z) return true;
+        }
+    }
+    return false;
+}
+
+__device__ __forceinline__ void sparse_count_hit(const PixelwiseArgs &a, PwSparseShared &S, int x, int y) {
+    const int fw = S.fx1 - S.fx0, fh = S.fy1 - S.fy0;
+    if ((long long)fw * fh <= kPwFootMax && x >= S.fx0 && x - S.fx0 < fw && y >= S.fy0 && y - S.fy0 < fh)
+        atomicAdd(&S.cnt[(y - S.fy0) * fw + (x - S.fx0)], 1u);
+    else
+        atomicAdd(&a.out[(long long)y * a.out_w + x], 1.0f);
+}
+
+// Step 3, out of line (its loops get the whole register budget).  When every offset owns a
+// rectangle of the same power-of-two size (zoom 1 away from the plane's edges), consecutive threads
+// take consecutive pixels of one offset -- neighbouring samples, similar cell ranges; otherwise each
+// thread takes the pixels of one offset (`parts` threads per offset when N < the CTA size).
+__device__ __noinline__ void sparse_samples(const PixelwiseArgs &a, PwSparseShared &S) {
+    const int tid = threadIdx.x, nthreads = blockDim.x;
+    unsigned long long slow = 0;
+    const int W = S.rw_min, H = S.rh_min;
+    const bool uniform = W == S.rw_max && H == S.rh_max && W > 0 && H > 0 && (W & (W - 1)) == 0 &&
+                         (H & (H - 1)) == 0 && W * H <= 1024;
+    if (uniform) {
+        const int lw = __ffs(W) - 1, lp = lw + __ffs(H) - 1;
+        const int total = a.n << lp;
+        for (int s = tid; s < total; s += nthreads) {
+            const int k = s >> lp, pix = s & ((1 << lp) - 1);
+            const int4 R = S.rect[k];
+            const float2 o = a.offs[k];
+            const int x = R.x + (pix & (W - 1)), y = R.z + (pix >> lw);
+            const float xg = xg_of(x, a.inv_zoom, o.x), yg = xg_of(y, a.inv_zoom, o.y);
+            const int j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
+            const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
+            if (sparse_sample_hit(a, S, xg, yg, j0, j1, slow)) sparse_count_hit(a, S, x, y);
+        }
+    } else {
+        const int parts = a.n >= nthreads ? 1 : nthreads / a.n;
+        for (int t = tid; t < a.n * parts; t += nthreads) {
+            const int k = t / parts, p = t % parts;
+            const int4 R = S.rect[k];
+            const float2 o = a.offs[k];
+            for (int y = R.z + p; y < R.w; y += parts) {
+                const float yg = xg_of(y, a.inv_zoom, o.y);
+                const int j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
+                const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
+                for (int x = R.x; x < R.y; x++)
+                    if (sparse_sample_hit(a, S, xg_of(x, a.inv_zoom, o.x), yg, j0, j1, slow)) sparse_count_hit(a, S, x, y);
+            }
+        }
+    }
+    if (slow) atomicAdd(&a.diag[0], slow);
+}
+
+// Step 2, out of line: the list of non-empty cells (column-major) with the rank before each mask
+// word, then their grain counts, CSR prefix and grains.  Returns false (uniformly) when the list or
+// the grains overflow their shared-memory buffers.
+__device__ __noinline__ bool sparse_stage(const PixelwiseArgs &a, PwSparseShared &S) {
+    using C = PwSparse;
+    const int tid = threadIdx.x, nthreads = blockDim.x;
+    const int Wc = S.Wc, Hc = S.Hc, hw = S.hw, wi0 = S.wi0, wj0 = S.wj0;
+    const int nwords = Wc * hw;
+    int nlist;
+    {
+        const int per = (nwords + nthreads - 1) / nthreads;
+        const int b = tid * per, e = min(nwords, b + per);
+        int local = 0;
+        for (int w = b; w < e; w++) local += __popc(S.mask2[w].x);
+        int total;
+        int run = block_excl_scan(local, S.wsum, &total);
+        nlist = total;
+        if (total <= C::kListMax) {
+            for (int w = b; w < e; w++) {
+                S.wrank[w] = (unsigned short)run;
+                unsigned m = S.mask2[w].x;
+                const int col = w / hw, row0 = (w - col * hw) * 32;
+                while (m) {
+                    const int bit = __ffs(m) - 1;
+                    m &= m - 1u;
+                    S.list[run++] = (unsigned short)(col * Hc + row0 + bit);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (nlist > C::kListMax) return false;
+    for (int t = tid; t < nlist; t += nthreads) {
+        const int c = S.list[t];
+        Xoshiro rng;
+        const uint32_t q = sparse_cell_count(a, wi0 + c / Hc, wj0 + c % Hc, &rng);
+        S.gstart[t] = (unsigned short)(q > 65535u ? 65535u : q);
+    }
+    __syncthreads();
+    int ngrains;
+    {
+        const int per = (nlist + nthreads - 1) / nthreads;
+        const int b = tid * per, e = min(nlist, b + per);
+        int local = 0;
+        for (int t = b; t < e; t++) local += S.gstart[t];
+        int total;
+        int run = block_excl_scan(local, S.wsum, &total);
+        ngrains = total;
+        if (total <= C::kGrainMax) {
+            for (int t = b; t < e; t++) {
+                const int q = S.gstart[t];
+                S.gstart[t] = (unsigned short)run;
+                run += q;
+            }
+            if (tid == 0) S.gstart[nlist] = (unsigned short)total;
+        }
+    }
+    __syncthreads();
+    if (ngrains > C::kGrainMax) return false;
+    const UniformF32 U = uniform_f32_new(0.0f, a.delta);
+    for (int t = tid; t < nlist; t += nthreads) {
+        const int c = S.list[t];
+        const int i = wi0 + c / Hc, j = wj0 + c % Hc;
+        const CellParam cp = a.cells[cell_pixel(a, i, j)];
+        const int base = S.gstart[t];
+        uint32_t q = (uint32_t)(S.gstart[t + 1] - base);
+        Xoshiro rng;
+        if (cp.thresh >= 0) {
+            // Knuth regime: the Poisson draw consumed exactly q + 1 uniforms; skip them.
+            rng = small_seed(cell_row_hash(cell_col_hash(a.seed, i), j));
+            for (uint32_t k = 0; k <= q; k++) (void)rng.next();
+        } else {
+            q = min(q, sparse_cell_count(a, i, j, &rng));
+        }
+        const float sx = FG_FMUL((float)i, a.delta), sy = FG_FMUL((float)j, a.delta);
+        for (uint32_t k = 0; k < q; k++) {
+            const float cx = FG_FADD(sx, uniform_f32_from(U, rng.next()));
+            const float cy = FG_FADD(sy, uniform_f32_from(U, rng.next()));
+            float r = a.lognorm ? sparse_radius(a, rng) : a.radius_mean;
+            if (r > a.rm) r = a.rm;
+            const float rr = (r <= 0.0f) ? -1.0f : FG_FMUL(r, r);  // -1 never passes the disk test
+            S.grains[base + k] = make_float4(cx, cy, rr, 0.0f);
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
+// One block of edge bs at block coordinates (bx, by) (all threads of the CTA; `smem_raw` holds
+// PwSparseShared): 0 rendered (or nothing to render), 1 left undone (its buffers would overflow:
+// nothing written), 2 stopped by cancellation.
+__device__ __noinline__ int pixelwise_sparse_block(const PixelwiseArgs &a, const PwSparseGrid &g, float bs, int bx,
+                                                   int by, unsigned char *smem_raw) {
     using C = PwSparse;
     PwSparseShared &S = *reinterpret_cast<PwSparseShared *>(smem_raw);
-    const int tid = threadIdx.x, nthreads = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nthreads >> 5;
+    const int tid = threadIdx.x, nthreads = blockDim.x, lane = tid & 31;
     // the cancellation word, read now and tested after the ownership pass (its latency overlaps it)
     int cancel_seen = 0;
     if (tid == 0 && a.cancel) cancel_seen = *(volatile int *)a.cancel;
 
-    const float X0 = FG_FMUL((float)sbx, g.bs), X1 = FG_FMUL((float)(sbx + 1), g.bs);
-    const float Y0 = FG_FMUL((float)sby, g.bs), Y1 = FG_FMUL((float)(sby + 1), g.bs);
+    const float X0 = FG_FMUL((float)bx, bs), X1 = FG_FMUL((float)(bx + 1), bs);
+    const float Y0 = FG_FMUL((float)by, bs), Y1 = FG_FMUL((float)(by + 1), bs);
     // Every owned sample has xg in [X0, X1) and computes its cell range with these same rounded,
     // monotone operations, so its range lies inside [wi0, wi1] x [wj0, wj1].
     const int wi0 = f2i_floor(FG_FDIV(FG_FSUB(X0, a.rm), a.delta));
@@ -107,17 +312,20 @@ __device__ __forceinline__ bool pixelwise_sparse_block(const PixelwiseArgs &a, c
     const int wj0 = f2i_floor(FG_FDIV(FG_FSUB(Y0, a.rm), a.delta));
     const int wj1 = f2i_floor(FG_FDIV(FG_FADD(Y1, a.rm), a.delta));
     const int Wc = wi1 - wi0 + 1, Hc = wj1 - wj0 + 1;
-    const int wpr = (Wc + 31) >> 5;
-    const bool fits = Wc > 0 && Hc > 0 && Hc <= C::kRowsMax && wpr * Hc <= C::kMaskWords;
+    const int hw = (Hc + 31) >> 5;  // mask words per window column
+    const bool fits = Wc > 0 && Hc > 0 && Hc <= C::kRowsMax && Wc * hw <= C::kMaskWords &&
+                      wi0 >= g.gi0 && wi1 < g.gi0 + g.gw && wj0 >= g.gj0 && wj1 < g.gj0 + 32 * (g.ghw - 1);
 
-    // ---- expected grains and non-empty cells of the window: lambda integrated over its rectangle (a
-    // cell takes the lambda of the pixel containing its origin; edge pixels extend outwards)
     if (tid == 0) {
+        S.wi0 = wi0; S.wi1 = wi1; S.wj0 = wj0; S.wj1 = wj1; S.Wc = Wc; S.Hc = Hc; S.hw = hw;
         S.est_grains = 0.0f;
         S.est_cells = 0.0f;
         S.fx0 = 0x7fffffff; S.fx1 = -1; S.fy0 = 0x7fffffff; S.fy1 = -1; S.nsamples = 0;
+        S.rw_min = 0x7fffffff; S.rw_max = -1; S.rh_min = 0x7fffffff; S.rh_max = -1;
     }
     __syncthreads();
+    // ---- expected grains and non-empty cells of the window: lambda integrated over its rectangle (a
+    // cell takes the lambda of the pixel containing its origin; edge pixels extend outwards)
     if (fits) {
         const float wx0 = FG_FMUL((float)wi0, a.delta), wx1 = FG_FMUL((float)(wi1 + 1), a.delta);
         const float wy0 = FG_FMUL((float)wj0, a.delta), wy1 = FG_FMUL((float)(wj1 + 1), a.delta);
@@ -146,9 +354,11 @@ __device__ __forceinline__ bool pixelwise_sparse_block(const PixelwiseArgs &a, c
             atomicAdd(&S.est_cells, ce);
         }
     }
-    // ---- ownership: rectangles per offset, sample total and pixel footprint (N <= kPwKChunk)
+    // ---- ownership: rectangles per offset, sample total, pixel footprint, rectangle size extremes
+    // (N <= kPwKChunk)
     {
         int lx0 = 0x7fffffff, lx1 = -1, ly0 = 0x7fffffff, ly1 = -1, ns = 0;
+        int wmin = 0x7fffffff, wmax = -1, hmin = 0x7fffffff, hmax = -1;
         for (int k = tid; k < a.n; k += nthreads) {
             const float2 o = a.offs[k];
             const int xa = first_at_least(X0, a.out_w, a.inv_zoom, a.zoom, o.x);
@@ -156,6 +366,8 @@ __device__ __forceinline__ bool pixelwise_sparse_block(const PixelwiseArgs &a, c
             const int ya = first_at_least(Y0, a.out_h, a.inv_zoom, a.zoom, o.y);
             const int ye = first_at_least(Y1, a.out_h, a.inv_zoom, a.zoom, o.y);
             S.rect[k] = make_int4(xa, xe, ya, ye);
+            wmin = min(wmin, xe - xa); wmax = max(wmax, xe - xa);
+            hmin = min(hmin, ye - ya); hmax = max(hmax, ye - ya);
             if (xe > xa && ye > ya) {
                 ns += (xe - xa) * (ye - ya);
                 lx0 = min(lx0, xa); lx1 = max(lx1, xe);
@@ -167,10 +379,20 @@ __device__ __forceinline__ bool pixelwise_sparse_block(const PixelwiseArgs &a, c
         lx1 = __reduce_max_sync(0xffffffffu, lx1);
         ly0 = __reduce_min_sync(0xffffffffu, ly0);
         ly1 = __reduce_max_sync(0xffffffffu, ly1);
-        if (lane == 0 && ns > 0) {
-            atomicAdd(&S.nsamples, ns);
-            atomicMin(&S.fx0, lx0); atomicMax(&S.fx1, lx1);
-            atomicMin(&S.fy0, ly0); atomicMax(&S.fy1, ly1);
+        wmin = __reduce_min_sync(0xffffffffu, wmin);
+        wmax = __reduce_max_sync(0xffffffffu, wmax);
+        hmin = __reduce_min_sync(0xffffffffu, hmin);
+        hmax = __reduce_max_sync(0xffffffffu, hmax);
+        if (lane == 0) {
+            if (ns > 0) {
+                atomicAdd(&S.nsamples, ns);
+                atomicMin(&S.fx0, lx0); atomicMax(&S.fx1, lx1);
+                atomicMin(&S.fy0, ly0); atomicMax(&S.fy1, ly1);
+            }
+            if (wmax >= 0) {  // the warp saw offsets
+                atomicMin(&S.rw_min, wmin); atomicMax(&S.rw_max, wmax);
+                atomicMin(&S.rh_min, hmin); atomicMax(&S.rh_max, hmax);
+            }
         }
     }
     if (tid == 0) {
@@ -178,195 +400,73 @@ __device__ __forceinline__ bool pixelwise_sparse_block(const PixelwiseArgs &a, c
         if (cancel_seen) *(volatile int *)(a.cancel + 1) = 1;
     }
     __syncthreads();
-    if (S.nsamples == 0 || S.stop) return false;
+    if (S.stop) return 2;
+    if (S.nsamples == 0) return 0;
     if (!fits || S.est_grains > 0.75f * (float)C::kGrainMax || S.est_cells > 0.75f * (float)C::kListMax)
-        return true;  // the fat pass takes the block's fat-grid blocks
-    const int fx0 = S.fx0, fy0 = S.fy0, fw = S.fx1 - S.fx0, fh = S.fy1 - S.fy0;
+        return 1;
+    const int fw = S.fx1 - S.fx0, fh = S.fy1 - S.fy0;
     const bool use_cnt = (long long)fw * fh <= kPwFootMax;
     if (use_cnt)
         for (int t = tid; t < fw * fh; t += nthreads) S.cnt[t] = 0u;
 
-    // ---- 1. emptiness bitmask: unit u = (column group u % wpr, row band u / wpr), one per warp in turn
+    // ---- 1. the window's bits from the plane's bitmask (word k of window column c: rows 32k .. 32k + 31)
     {
-        const int nbands = (Hc + C::kRowBand - 1) / C::kRowBand;
-        for (int u = warp; u < wpr * nbands; u += nwarps) {
-            const int cg = u % wpr, band = u / wpr;
-            const int ci = cg * 32 + lane;
-            const bool valid = ci < Wc;
-            const int i = wi0 + (valid ? ci : Wc - 1);
-            const uint64_t colh = cell_col_hash(a.seed, i);
-            long long ix = (long long)floorf(FG_FMUL((float)i, a.delta));
-            ix = ix < 0 ? 0 : (ix > a.in_w - 1 ? a.in_w - 1 : ix);
-            int iy_prev = -1;
-            long long thresh = 0;
-            const int r0 = band * C::kRowBand, r1 = min(Hc, r0 + C::kRowBand);
-            for (int r = r0; r < r1; r++) {
-                const int j = wj0 + r;
-                long long iy = (long long)floorf(FG_FMUL((float)j, a.delta));
-                iy = iy < 0 ? 0 : (iy > a.in_h - 1 ? a.in_h - 1 : iy);
-                if ((int)iy != iy_prev) {
-                    iy_prev = (int)iy;
-                    thresh = a.cells[iy * a.in_w + ix].thresh;
-                }
-                const long long v = (long long)(small_first_u64(cell_row_hash(colh, j)) >> 11);
-                const unsigned word = __ballot_sync(0xffffffffu, valid && v > thresh);
-                if (lane == 0) S.mask[r * wpr + cg] = word;
-            }
+        const int rb = wj0 - g.gj0, rw = rb >> 5, rs = rb & 31;
+        const unsigned tail = (Hc & 31) ? ((1u << (Hc & 31)) - 1u) : 0xffffffffu;
+        for (int idx = tid; idx < Wc * hw; idx += nthreads) {
+            const int k = idx / Wc, c = idx - k * Wc;  // consecutive threads: consecutive columns
+            const int gc = wi0 - g.gi0 + c;
+            const unsigned lo = g.cellmask[(long long)(rw + k) * g.gw + gc];
+            const unsigned hi = rs ? g.cellmask[(long long)(rw + k + 1) * g.gw + gc] : 0u;
+            unsigned word = __funnelshift_r(lo, hi, rs);
+            if (k == hw - 1) word &= tail;
+            S.mask2[c * hw + k].x = word;
         }
+        __syncthreads();
+        for (int w = tid; w < Wc * hw; w += nthreads) {
+            const int k = w % hw;
+            S.mask2[w].y = k + 1 < hw ? S.mask2[w + 1].x : 0u;
+        }
+        __syncthreads();
     }
-    __syncthreads();
 
-    // ---- 2. list of the non-empty cells (row-major), the rank before each mask word
-    const int nwords = wpr * Hc;
-    int nlist;
-    {
-        const int per = (nwords + nthreads - 1) / nthreads;
-        const int b = tid * per, e = min(nwords, b + per);
-        int local = 0;
-        for (int w = b; w < e; w++) local += __popc(S.mask[w]);
-        int total;
-        int run = block_excl_scan(local, S.wsum, &total);
-        nlist = total;
-        if (total <= C::kListMax) {
-            for (int w = b; w < e; w++) {
-                S.wrank[w] = (unsigned short)run;
-                unsigned m = S.mask[w];
-                const int row = w / wpr, col0 = (w - row * wpr) * 32;
-                while (m) {
-                    const int bit = __ffs(m) - 1;
-                    m &= m - 1u;
-                    S.list[run++] = (unsigned short)(row * Wc + col0 + bit);
-                }
-            }
-        }
-    }
-    __syncthreads();
-    if (nlist > C::kListMax) return true;
+    // ---- 2. non-empty cells, their counts and grains
+    if (!sparse_stage(a, S)) return 1;
 
-    // ---- grain counts of the listed cells, their CSR prefix, then the grains
-    for (int t = tid; t < nlist; t += nthreads) {
-        const int c = S.list[t];
-        Xoshiro rng;
-        const uint32_t q = sparse_cell_count(a, wi0 + c % Wc, wj0 + c / Wc, &rng);
-        S.gstart[t] = (unsigned short)(q > 65535u ? 65535u : q);
-    }
-    __syncthreads();
-    int ngrains;
-    {
-        const int per = (nlist + nthreads - 1) / nthreads;
-        const int b = tid * per, e = min(nlist, b + per);
-        int local = 0;
-        for (int t = b; t < e; t++) local += S.gstart[t];
-        int total;
-        int run = block_excl_scan(local, S.wsum, &total);
-        ngrains = total;
-        if (total <= C::kGrainMax) {
-            for (int t = b; t < e; t++) {
-                const int q = S.gstart[t];
-                S.gstart[t] = (unsigned short)run;
-                run += q;
-            }
-            if (tid == 0) S.gstart[nlist] = (unsigned short)total;
-        }
-    }
-    __syncthreads();
-    if (ngrains > C::kGrainMax) return true;
-    {
-        const UniformF32 U = uniform_f32_new(0.0f, a.delta);
-        for (int t = tid; t < nlist; t += nthreads) {
-            const int c = S.list[t];
-            const int i = wi0 + c % Wc, j = wj0 + c / Wc;
-            const CellParam cp = a.cells[cell_pixel(a, i, j)];
-            const int base = S.gstart[t];
-            uint32_t q = (uint32_t)(S.gstart[t + 1] - base);
-            Xoshiro rng;
-            if (cp.thresh >= 0) {
-                // Knuth regime: the Poisson draw consumed exactly q + 1 uniforms; skip them.
-                rng = small_seed(cell_row_hash(cell_col_hash(a.seed, i), j));
-                for (uint32_t k = 0; k <= q; k++) (void)rng.next();
-            } else {
-                q = min(q, sparse_cell_count(a, i, j, &rng));
-            }
-            const float sx = FG_FMUL((float)i, a.delta), sy = FG_FMUL((float)j, a.delta);
-            for (uint32_t k = 0; k < q; k++) {
-                const float cx = FG_FADD(sx, uniform_f32_from(U, rng.next()));
-                const float cy = FG_FADD(sy, uniform_f32_from(U, rng.next()));
-                float r = a.lognorm ? sparse_radius(a, rng) : a.radius_mean;
-                if (r > a.rm) r = a.rm;
-                const float rr = (r <= 0.0f) ? -1.0f : FG_FMUL(r, r);  // -1 never passes the disk test
-                S.grains[base + k] = make_float4(cx, cy, rr, 0.0f);
-            }
-        }
-    }
-    __syncthreads();
-
-    // ---- 3. the owned samples: offset k's pixel rectangle, shared by `parts` threads by rows
-    {
-        const int parts = a.n >= nthreads ? 1 : nthreads / a.n;
-        unsigned long long slow = 0;
-        for (int t = tid; t < a.n * parts; t += nthreads) {
-            const int k = t / parts, p = t % parts;
-            const int4 R = S.rect[k];
-            const float2 o = a.offs[k];
-            for (int y = R.z + p; y < R.w; y += parts) {
-                const float yg = xg_of(y, a.inv_zoom, o.y);
-                const int j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
-                const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
-                for (int x = R.x; x < R.y; x++) {
-                    const float xg = xg_of(x, a.inv_zoom, o.x);
-                    bool hit = false;
-                    if (a.rm > 0.0f) {
-                        const int i0 = f2i_floor(FG_FDIV(FG_FSUB(xg, a.rm), a.delta));
-                        const int i1 = f2i_floor(FG_FDIV(FG_FADD(xg, a.rm), a.delta));
-                        if (i0 <= i1 && j0 <= j1) {
-                            if (i0 >= wi0 && i1 <= wi1 && j0 >= wj0 && j1 <= wj1 && i1 - i0 < 32) {
-                                const int c0 = i0 - wi0, w0 = c0 >> 5, b0 = c0 & 31;
-                                const unsigned span = (unsigned)(i1 - i0);
-                                const unsigned keep = span == 31u ? 0xffffffffu : ((2u << span) - 1u);
-                                for (int j = j0; j <= j1 && !hit; j++) {
-                                    const int wbase = (j - wj0) * wpr + w0;
-                                    const unsigned lo = S.mask[wbase];
-                                    const unsigned hi = (w0 + 1 < wpr) ? S.mask[wbase + 1] : 0u;
-                                    const unsigned bits = __funnelshift_r(lo, hi, b0) & keep;
-                                    if (!bits) continue;
-                                    const int rank = S.wrank[wbase] + __popc(lo & ((1u << b0) - 1u));
-                                    const int gs = S.gstart[rank], ge = S.gstart[rank + __popc(bits)];
-                                    for (int gi = gs; gi < ge; gi++) {
-                                        const float4 G = S.grains[gi];
-                                        const float dx = FG_FSUB(xg, G.x), dy = FG_FSUB(yg, G.y);
-                                        if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= G.z) {
-                                            hit = true;
-                                            break;
-                                        }
-                                    }
-                                }
-                            } else {
-                                slow++;
-                                hit = sparse_regen_sample(a, xg, yg, i0, i1, j0, j1);
-                            }
-                        }
-                    }
-                    if (hit) {
-                        const bool in_foot = use_cnt && x >= fx0 && x - fx0 < fw && y >= fy0 && y - fy0 < fh;
-                        if (in_foot) atomicAdd(&S.cnt[(y - fy0) * fw + (x - fx0)], 1u);
-                        else atomicAdd(&a.out[(long long)y * a.out_w + x], 1.0f);
-                    }
-                }
-            }
-        }
-        if (slow) atomicAdd(&a.diag[0], slow);
-    }
+    // ---- 3. the owned samples
+    sparse_samples(a, S);
     __syncthreads();
 
     // ---- 4. flush the per-pixel counts
     if (use_cnt) {
         for (int t = tid; t < fw * fh; t += nthreads) {
             const unsigned c = S.cnt[t];
-            if (c) atomicAdd(&a.out[(long long)(fy0 + t / fw) * a.out_w + (fx0 + t % fw)], (float)c);
+            if (c) atomicAdd(&a.out[(long long)(S.fy0 + t / fw) * a.out_w + (S.fx0 + t % fw)], (float)c);
         }
     }
     if (tid == 0) atomicAdd(&a.diag[3], 1ull);
-    return false;
+    return 0;
+}
+
+// Sparse block (sbx, sby): whole, or -- when it overflows -- as its fat-grid blocks one after another;
+// a fat-grid block that overflows too is appended to the deferred list for the fat pass (each fat-grid
+// block is either rendered here or listed, never both).
+__device__ __forceinline__ void pixelwise_sparse_root(const PixelwiseArgs &a, const PwSparseGrid &g, int sbx, int sby,
+                                                      int nby, int *list, unsigned char *smem_raw) {
+    const int st = pixelwise_sparse_block(a, g, g.bs, sbx, sby, smem_raw);
+    if (st != 1) return;
+    if (g.ratio == 1) {
+        if (threadIdx.x == 0) sparse_defer(a, g, sbx, sby, nby, list);
+        return;
+    }
+    for (int q = 0; q < g.ratio * g.ratio; q++) {
+        const int bx = sbx * g.ratio + q % g.ratio, by = sby * g.ratio + q / g.ratio;
+        if (bx < a.bx0 || bx >= a.bx0 + a.nbx || by < a.by0 || by >= a.by0 + nby) continue;
+        __syncthreads();  // the previous block's shared state is no longer read
+        const int sq = pixelwise_sparse_block(a, g, a.bsize, bx, by, smem_raw);
+        if (sq == 2) return;
+        if (sq == 1 && threadIdx.x == 0) list[1 + atomicAdd(list, 1)] = (by - a.by0) * a.nbx + (bx - a.bx0);
+    }
 }
 
 }  // namespace fg
