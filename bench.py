@@ -559,8 +559,8 @@ def plain_line(wl_name, steps, warmup, rank=0, world=1, dist=None, cpu=True, e2e
     sp = stream.cuda_stream
     offs = np.ascontiguousarray(derived.offsets if wl["algo"] == "grain" else derived.offsets_input, np.float32)
     fn = L.fg_render_grainwise_async if wl["algo"] == "grain" else L.fg_render_pixelwise_async
-    # grain: tile costs, tile order, persistent tiles, popcount; pixel: cell table, per-sample kernel or
-    # lean + fat block passes, epilogue
+    # grain: tile costs, tile order, persistent tiles, popcount; pixel: cell table, then the per-sample
+    # kernel, or the emptiness bitmask + sparse and fat block passes, or lean + fat block passes; epilogue
     launches_per_plane = 4 if wl["algo"] == "grain" else fg.pixelwise_kernel_count(params, derived)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -683,9 +683,11 @@ def plain_line(wl_name, steps, warmup, rank=0, world=1, dist=None, cpu=True, e2e
         line["roofline"] = {"bound": "sm_issue", "achieved": ach / 1e12, "peak": peak / 1e12, "unit": "Tlane-op/s",
                             "frac": ach / peak,
                             "traffic": PIXELWISE_DRAM_BYTES_PER_OUT_PX * ow * oh,
-                            "traffic_basis": "ncu dram bytes of the lean and deferred pixel-wise block passes on "
-                                             "plane 0 of the 4096^2 x 3 frame, scaled by output pixels",
-                            "kernel": "pixelwise_kernel (launch_ms: the whole plane)", "launch_ms": launch_ms,
+                            "traffic_basis": "ncu dram bytes of the plane's kernels (cell table, emptiness bitmask, "
+                                             "sparse and deferred block passes, epilogue) on plane 0 of the "
+                                             "4096^2 x 3 frame, scaled by output pixels",
+                            "kernel": "cell_mask_kernel + pixelwise_sparse_kernel + pixelwise_deferred_kernel "
+                                      "(launch_ms: the whole render call of a plane)", "launch_ms": launch_ms,
                             "lane_ops_per_launch": [o["total"] for o in ops], "model_terms": ops[0],
                             "peak_basis": peak_basis}
     return line

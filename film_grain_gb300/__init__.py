@@ -459,8 +459,8 @@ def render_grainwise(lam, params: Params, derived: Derived, cancel: Optional[Cal
 
 
 def pixelwise_kernel_count(params: "Params", derived: "Derived") -> int:
-    """Kernel launches one pixel-wise render of these params makes: 3 on the per-sample kernel, 4 on the
-    block kernels."""
+    """Kernel launches one pixel-wise render of these params makes: 3 on the per-sample kernel, 5 on the
+    sparse block pass (with the plane's emptiness bitmask), 4 on the lean block pass."""
     offs = np.ascontiguousarray(derived.offsets_input, np.float32)
     n = ctypes.c_int32()
     _raise(lib().fg_pixelwise_kernel_count(params.c, derived._c, offs.ctypes.data, ctypes.byref(n)))

@@ -151,8 +151,8 @@ static int sm_count() {
 size_t pixelwise_cellmask_bytes(const PixelwiseArgs &a, int nby) {
     if (pixelwise_prefers_regen(a)) return 0;
     PwSparseGrid g;
-    const int sms = sm_count();
-    if (sms <= 0 || !plan_sparse(a, nby, sms, &g)) return 0;
+    const int sms = sm_count();  // without a device (planning only): the GB300's 152
+    if (!plan_sparse(a, nby, sms > 0 ? sms : 152, &g)) return 0;
     return (size_t)g.gw * g.ghw * sizeof(unsigned int);
 }
 

@@ -119,12 +119,25 @@ FG_HD uint32_t rotr32(uint32_t x, uint32_t r) {
     return r ? (x >> r) | (x << (32u - r)) : x;
 #endif
 }
-// Seed word k (1..8) of seed_from_u64(h).
+FG_HD uint32_t funnel_r32(uint32_t lo, uint32_t hi, int s) {  // low word of (hi:lo) >> s, 0 < s < 32
+#ifdef __CUDA_ARCH__
+    return __funnelshift_r(lo, hi, s);
+#else
+    return (lo >> s) | (hi << (32 - s));
+#endif
+}
+// Seed word k (1..8) of seed_from_u64(h).  The state st = a*h + c (mod 2^64) in 32-bit halves: the
+// low product with c added in one wide multiply-add, the cross products into the high half; the
+// output needs bits 27..58 of st ^ (st >> 18), i.e. (st >> 27) ^ (st >> 45) cut to 32 bits, rotated
+// right by st >> 59.
 template <int K>
 FG_HD uint32_t pcg_word(uint64_t h) {
     constexpr uint64_t a = pcg_jump_mul(K), c = pcg_jump_add(K);
-    const uint64_t st = a * h + c;
-    return rotr32((uint32_t)(((st >> 18) ^ st) >> 27), (uint32_t)(st >> 59));
+    const uint32_t hl = (uint32_t)h, hh = (uint32_t)(h >> 32);
+    const uint64_t w = (uint64_t)hl * (uint32_t)a + c;
+    const uint32_t L = (uint32_t)w;
+    const uint32_t H = (uint32_t)(w >> 32) + hl * (uint32_t)(a >> 32) + hh * (uint32_t)a;
+    return rotr32(funnel_r32(L, H, 27) ^ (H >> 13), H >> 27);
 }
 FG_HD uint64_t pcg_pair(uint32_t lo, uint32_t hi) { return (uint64_t)lo | ((uint64_t)hi << 32); }
 FG_HD Xoshiro small_seed_zero() {
