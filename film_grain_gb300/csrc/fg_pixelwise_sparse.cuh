@@ -70,19 +70,19 @@ __device__ __forceinline__ void cell_mask_word(const PixelwiseArgs &a, const PwS
     const int c = (int)(t % g.gw), k = (int)(t / g.gw);
     const int i = g.gi0 + c;
     const uint64_t colh = cell_col_hash(a.seed, i);
-    long long ix = (long long)floorf(FG_FMUL((float)i, a.delta));
-    ix = ix < 0 ? 0 : (ix > a.in_w - 1 ? a.in_w - 1 : ix);
+    // the cell's lambda pixel, clamped to the plane (cell_pixel); cell coordinates stay far inside int,
+    // so the clamp is done on floats and the conversion is a 32-bit one
+    const int ix = (int)fminf(fmaxf(floorf(FG_FMUL((float)i, a.delta)), 0.0f), (float)(a.in_w - 1));
     int iy_prev = -1;
     long long thresh = 0;
     unsigned int word = 0;
 #pragma unroll 4
     for (int r = 0; r < 32; r++) {
         const int j = g.gj0 + 32 * k + r;
-        long long iy = (long long)floorf(FG_FMUL((float)j, a.delta));
-        iy = iy < 0 ? 0 : (iy > a.in_h - 1 ? a.in_h - 1 : iy);
-        if ((int)iy != iy_prev) {
-            iy_prev = (int)iy;
-            thresh = a.cells[iy * a.in_w + ix].thresh;
+        const int iy = (int)fminf(fmaxf(floorf(FG_FMUL((float)j, a.delta)), 0.0f), (float)(a.in_h - 1));
+        if (iy != iy_prev) {
+            iy_prev = iy;
+            thresh = a.cells[(long long)iy * a.in_w + ix].thresh;
         }
         const long long v = (long long)(small_first_u64(cell_row_hash(colh, j)) >> 11);
         word |= (v > thresh ? 1u : 0u) << r;
@@ -97,12 +97,8 @@ __device__ __noinline__ bool sparse_regen_sample(const PixelwiseArgs &a, float x
     return eval_regen(a, U, xg, yg, i0, i1, j0, j1);
 }
 
-// One grain radius (out of line: the lognormal draw is long and runs once per staged grain).
-__device__ __noinline__ float sparse_radius(const PixelwiseArgs &a, Xoshiro &rng) { return radius_draw(a, rng); }
-
-// Grain count of cell (i, j) with the stream left after the Poisson draws (out of line: the rejection
-// regime is long).
-__device__ __noinline__ uint32_t sparse_cell_count(const PixelwiseArgs &a, int i, int j, Xoshiro *rng) {
+// Grain count of cell (i, j) with the stream left after the Poisson draws.
+__device__ __forceinline__ uint32_t sparse_cell_count(const PixelwiseArgs &a, int i, int j, Xoshiro *rng) {
     const CellParam cp = a.cells[cell_pixel(a, i, j)];
     Xoshiro r;
     const uint32_t q = cell_count(a.seed, i, j, cp, r);
@@ -120,21 +116,19 @@ __device__ __forceinline__ void sparse_defer(const PixelwiseArgs &a, const PwSpa
     }
 }
 
-// Whether sample (xg, yg) is covered: the reference's cell range (src/pixelwise.rs:55-58), one
-// 64-bit shared load per cell column for the bits of rows j0..j1, the disk test on the grains of the
-// set bits (src/pixelwise.rs:96-99); samples whose range leaves the window take the per-sample loop.
-__device__ __forceinline__ bool sparse_sample_hit(const PixelwiseArgs &a, const PwSparseShared &S, float xg, float yg,
-                                                  int j0, int j1, unsigned long long &slow) {
-    if (!(a.rm > 0.0f)) return false;
+// Sample (xg, yg): 0 not covered, 1 covered, 2 its cell range leaves the window (the per-sample loop
+// decides it, in a second pass).  The reference's cell range (src/pixelwise.rs:55-58), one 64-bit
+// shared load per cell column for the bits of rows j0..j1, the disk test on the grains of the set bits
+// (src/pixelwise.rs:96-99).
+__device__ __forceinline__ int sparse_sample_hit(const PixelwiseArgs &a, const PwSparseShared &S, float xg, float yg,
+                                                 int j0, int j1) {
+    if (!(a.rm > 0.0f)) return 0;
     const int i0 = f2i_floor(FG_FDIV(FG_FSUB(xg, a.rm), a.delta));
     const int i1 = f2i_floor(FG_FDIV(FG_FADD(xg, a.rm), a.delta));
-    if (i0 > i1 || j0 > j1) return false;  // no cell (src/pixelwise.rs:60-62)
+    if (i0 > i1 || j0 > j1) return 0;  // no cell (src/pixelwise.rs:60-62)
     const int wi0 = S.wi0, wj0 = S.wj0, hw = S.hw;
     const unsigned span = (unsigned)(j1 - j0);
-    if (i0 < wi0 || i1 > S.wi1 || j0 < wj0 || j1 > S.wj1 || span >= 32u) {
-        slow++;
-        return sparse_regen_sample(a, xg, yg, i0, i1, j0, j1);
-    }
+    if (i0 < wi0 || i1 > S.wi1 || j0 < wj0 || j1 > S.wj1 || span >= 32u) return 2;
     const int r0 = j0 - wj0, b0 = r0 & 31;
     const unsigned keep = (2u << span) - 1u;  // span <= 31: 2u << 31 wraps to 0 and keep is all ones
     const unsigned below = (1u << b0) - 1u;
@@ -148,11 +142,15 @@ __device__ __forceinline__ bool sparse_sample_hit(const PixelwiseArgs &a, const 
         for (int g = S.gstart[rank]; g < ge; g++) {
             const float4 G = S.grains[g];
             const float dx = FG_FSUB(xg, G.x), dy = FG_FSUB(yg, G.y);
-            if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= G.z) return true;
+            if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= G.z) return 1;
         }
     }
-    return false;
+    return 0;
 }
+
+// The second pass over a thread's samples: the ones whose range left the window.
+__device__ __noinline__ void sparse_slow_sample(const PixelwiseArgs &a, PwSparseShared &S, float xg, float yg, int x,
+                                                int y);
 
 __device__ __forceinline__ void sparse_count_hit(const PixelwiseArgs &a, PwSparseShared &S, int x, int y) {
     const int fw = S.fx1 - S.fx0, fh = S.fy1 - S.fy0;
@@ -166,9 +164,12 @@ __device__ __forceinline__ void sparse_count_hit(const PixelwiseArgs &a, PwSpars
 // rectangle of the same power-of-two size (zoom 1 away from the plane's edges), consecutive threads
 // take consecutive pixels of one offset -- neighbouring samples, similar cell ranges; otherwise each
 // thread takes the pixels of one offset (`parts` threads per offset when N < the CTA size).
-__device__ __noinline__ void sparse_samples(const PixelwiseArgs &a, PwSparseShared &S) {
+// One pass over the thread's samples: pass 0 evaluates every sample from the staged window and counts
+// the ones whose range leaves it; pass 1 sends exactly those to the per-sample loop.
+template <int kPass>
+__device__ __forceinline__ unsigned sparse_sample_pass(const PixelwiseArgs &a, PwSparseShared &S) {
     const int tid = threadIdx.x, nthreads = blockDim.x;
-    unsigned long long slow = 0;
+    unsigned slow = 0;
     const int W = S.rw_min, H = S.rh_min;
     const bool uniform = W == S.rw_max && H == S.rh_max && W > 0 && H > 0 && (W & (W - 1)) == 0 &&
                          (H & (H - 1)) == 0 && W * H <= 1024;
@@ -183,7 +184,13 @@ __device__ __noinline__ void sparse_samples(const PixelwiseArgs &a, PwSparseShar
             const float xg = xg_of(x, a.inv_zoom, o.x), yg = xg_of(y, a.inv_zoom, o.y);
             const int j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
             const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
-            if (sparse_sample_hit(a, S, xg, yg, j0, j1, slow)) sparse_count_hit(a, S, x, y);
+            const int h = sparse_sample_hit(a, S, xg, yg, j0, j1);
+            if (kPass == 0) {
+                if (h == 1) sparse_count_hit(a, S, x, y);
+                slow += h == 2;
+            } else if (h == 2) {
+                sparse_slow_sample(a, S, xg, yg, x, y);
+            }
         }
     } else {
         const int parts = a.n >= nthreads ? 1 : nthreads / a.n;
@@ -195,12 +202,37 @@ __device__ __noinline__ void sparse_samples(const PixelwiseArgs &a, PwSparseShar
                 const float yg = xg_of(y, a.inv_zoom, o.y);
                 const int j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
                 const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
-                for (int x = R.x; x < R.y; x++)
-                    if (sparse_sample_hit(a, S, xg_of(x, a.inv_zoom, o.x), yg, j0, j1, slow)) sparse_count_hit(a, S, x, y);
+                for (int x = R.x; x < R.y; x++) {
+                    const float xg = xg_of(x, a.inv_zoom, o.x);
+                    const int h = sparse_sample_hit(a, S, xg, yg, j0, j1);
+                    if (kPass == 0) {
+                        if (h == 1) sparse_count_hit(a, S, x, y);
+                        slow += h == 2;
+                    } else if (h == 2) {
+                        sparse_slow_sample(a, S, xg, yg, x, y);
+                    }
+                }
             }
         }
     }
-    if (slow) atomicAdd(&a.diag[0], slow);
+    return slow;
+}
+
+__device__ __noinline__ void sparse_samples(const PixelwiseArgs &a, PwSparseShared &S) {
+    const unsigned slow = sparse_sample_pass<0>(a, S);
+    if (__syncthreads_or(slow != 0)) {
+        if (slow) atomicAdd(&a.diag[0], (unsigned long long)slow);
+        sparse_sample_pass<1>(a, S);
+    }
+}
+
+__device__ __noinline__ void sparse_slow_sample(const PixelwiseArgs &a, PwSparseShared &S, float xg, float yg, int x,
+                                                int y) {
+    const int i0 = f2i_floor(FG_FDIV(FG_FSUB(xg, a.rm), a.delta));
+    const int i1 = f2i_floor(FG_FDIV(FG_FADD(xg, a.rm), a.delta));
+    const int j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
+    const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
+    if (sparse_regen_sample(a, xg, yg, i0, i1, j0, j1)) sparse_count_hit(a, S, x, y);
 }
 
 // Step 2, out of line: the list of non-empty cells (column-major) with the rank before each mask
@@ -281,7 +313,7 @@ __device__ __noinline__ bool sparse_stage(const PixelwiseArgs &a, PwSparseShared
         for (uint32_t k = 0; k < q; k++) {
             const float cx = FG_FADD(sx, uniform_f32_from(U, rng.next()));
             const float cy = FG_FADD(sy, uniform_f32_from(U, rng.next()));
-            float r = a.lognorm ? sparse_radius(a, rng) : a.radius_mean;
+            float r = radius_draw(a, rng);
             if (r > a.rm) r = a.rm;
             const float rr = (r <= 0.0f) ? -1.0f : FG_FMUL(r, r);  // -1 never passes the disk test
             S.grains[base + k] = make_float4(cx, cy, rr, 0.0f);
