@@ -650,7 +650,7 @@ FG_API fg_status fg_pixelwise_kernel_count(const fg_params *params, const fg_der
     if (st != FG_OK) return st;
     const PwPlan pl = plan_pixelwise(*params, *derived, offsets_input, 4);
     const PixelwiseArgs a = pixelwise_args(*params, *derived, pl, nullptr, nullptr, nullptr, nullptr, nullptr);
-    *out = pixelwise_prefers_regen(a) ? 3 : (pixelwise_cellmask_bytes(a, pl.nby) ? 5 : 4);
+    *out = pixelwise_prefers_regen(a) ? 3 : (pixelwise_cellmask_bytes(a, pl.nby) ? 6 : 4);
     clear_error();
     return FG_OK;
 }

@@ -90,6 +90,26 @@ __global__ void __launch_bounds__(PwSparse::kThreads, PwSparse::kCtasPerSm)
     pixelwise_sparse_root(a, g, sbx, sby, nby, list, smem_raw);
 }
 
+// The offsets in ascending x (ties by index: a permutation even with NaNs), for the sparse pass's
+// lanes (sparse_sample_pass).  One CTA; n <= kPwKChunk.
+__device__ __forceinline__ unsigned offset_sort_key(float v) {
+    const unsigned b = __float_as_uint(v);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);  // the float order as an unsigned order
+}
+__global__ void __launch_bounds__(256) sort_offsets_kernel(const float2 *__restrict__ offs, int n,
+                                                           float2 *__restrict__ sorted) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const float2 o = offs[k];
+        const unsigned key = offset_sort_key(o.x);
+        int rank = 0;
+        for (int j = 0; j < n; j++) {
+            const unsigned kj = offset_sort_key(offs[j].x);
+            rank += (kj < key || (kj == key && j < k)) ? 1 : 0;
+        }
+        sorted[rank] = o;
+    }
+}
+
 // The plane's emptiness bitmask (pixelwise_sparse_block step 0): one thread per mask word.
 __global__ void __launch_bounds__(256) cell_mask_kernel(const __grid_constant__ PixelwiseArgs a, const PwSparseGrid g,
                                                         unsigned int *__restrict__ cellmask) {
@@ -115,7 +135,7 @@ static bool plan_sparse(const PixelwiseArgs &a, int nby, int sms, PwSparseGrid *
     for (int R = 4; R >= 1; R >>= 1) {
         const float bs = a.bsize * (float)R;
         const double edge = std::floor(((double)bs + 2.0 * a.rm) / a.delta) + 3.0;
-        const double wpr = std::ceil(edge / 32.0);
+        const double wpr = (double)sparse_col_stride((int)std::ceil(edge / 32.0));
         if (edge > PwSparse::kRowsMax || wpr * edge > PwSparse::kMaskWords) continue;
         const int sbx0 = floor_div(a.bx0, R), sbx1 = floor_div(a.bx0 + a.nbx - 1, R);
         const int sby0 = floor_div(a.by0, R), sby1 = floor_div(a.by0 + nby - 1, R);
@@ -148,12 +168,17 @@ static int sm_count() {
     return sms;
 }
 
+// The sparse pass's scratch: the bitmask, then (16-byte aligned) the offsets sorted by x.
+static size_t sparse_mask_bytes(const PwSparseGrid &g) {
+    return ((size_t)g.gw * g.ghw * sizeof(unsigned int) + 15) & ~(size_t)15;
+}
+
 size_t pixelwise_cellmask_bytes(const PixelwiseArgs &a, int nby) {
     if (pixelwise_prefers_regen(a)) return 0;
     PwSparseGrid g;
     const int sms = sm_count();  // without a device (planning only): the GB300's 152
     if (!plan_sparse(a, nby, sms > 0 ? sms : 152, &g)) return 0;
-    return (size_t)g.gw * g.ghw * sizeof(unsigned int);
+    return sparse_mask_bytes(g) + (size_t)a.n * sizeof(float2);
 }
 
 // The root blocks the lean pass deferred, in fat CTAs: persistent, each CTA taking the next listed
@@ -242,11 +267,14 @@ cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, unsign
         g.cellmask = cellmask;
         const long long words = (long long)g.gw * g.ghw;
         cell_mask_kernel<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(a, g, cellmask);
+        PixelwiseArgs as = a;  // the sparse pass reads the offsets sorted by x
+        as.offs = reinterpret_cast<const float2 *>(reinterpret_cast<char *>(cellmask) + sparse_mask_bytes(g));
+        sort_offsets_kernel<<<1, 256, 0, s>>>(a.offs, a.n, const_cast<float2 *>(as.offs));
         const size_t sparse_smem = sizeof(PwSparseShared);
         e = set_smem(pixelwise_sparse_kernel, sparse_smem);
         if (e != cudaSuccess) return e;
         pixelwise_sparse_kernel<<<(unsigned)((long long)g.nsbx * g.nsby), PwSparse::kThreads, sparse_smem, s>>>(
-            a, g, nby, defer + 1);
+            as, g, nby, defer + 1);
     } else {
         pixelwise_kernel<PwLean><<<(unsigned)nblocks, PwLean::kThreads, lean_smem, s>>>(a, defer + 1);
     }

@@ -32,23 +32,43 @@ struct PwSparse {
     static constexpr int kThreads = 256, kCtasPerSm = 3;
     static constexpr int kGrainMax = 2048;   // staged grains
     static constexpr int kListMax = 2048;    // non-empty cells of the window
-    static constexpr int kMaskWords = 1024;  // window bitmask (32768 cells)
+    static constexpr int kMaskWords = 1280;  // window bitmask, columns an odd number of words apart
     static constexpr int kRowsMax = 256;     // window rows
+    static constexpr int kRangeSlots = 4;    // tabulated cell ranges per offset and axis
 };
+
+// Mask words per window column in shared memory: the column's words rounded up to an odd count, so
+// that lanes reading the same word row of columns a multiple of 8 apart meet on different banks.
+__host__ __device__ __forceinline__ int sparse_col_stride(int hw) { return hw | 1; }
+
+// A sample's cell range on one axis, relative to the window [w0, w1] (at most kMaskWords cells): low
+// 11 bits the first cell - w0, high 5 bits the last cell - the first; kRangeSlow when the range leaves
+// the window or spans more than 32 cells (the per-sample loop decides such samples).
+constexpr unsigned kRangeSlow = 0xFFFFu;
+__device__ __forceinline__ unsigned sparse_range_code(float g, float rm, float delta, int w0, int w1) {
+    const int c0 = f2i_floor(FG_FDIV(FG_FSUB(g, rm), delta));  // src/pixelwise.rs:55-58
+    const int c1 = f2i_floor(FG_FDIV(FG_FADD(g, rm), delta));
+    if (c0 < w0 || c1 > w1 || c1 < c0 || c1 - c0 > 31) return kRangeSlow;
+    return (unsigned)(c0 - w0) | ((unsigned)(c1 - c0) << 11);
+}
 
 struct PwSparseShared {
     float4 grains[PwSparse::kGrainMax];
     uint2 mask2[PwSparse::kMaskWords];           // (word w, the next word of the same column or 0)
     unsigned short wrank[PwSparse::kMaskWords];  // non-empty cells before each mask word (column-major)
     unsigned short list[PwSparse::kListMax];     // non-empty cells: window index i * Hc + j, column-major
-    unsigned short gstart[PwSparse::kListMax + 1];
+    unsigned int gsc[PwSparse::kListMax];        // per listed cell: first grain | grain count << 16
     int4 rect[kPwKChunk];                       // owned pixel rectangle per offset: xa, xe, ya, ye
+    // cell ranges (sparse_range_code) of the first kRangeSlots columns and rows of each offset's
+    // rectangle: entry [slot * n + k]
+    unsigned short range_x[PwSparse::kRangeSlots * kPwKChunk], range_y[PwSparse::kRangeSlots * kPwKChunk];
     unsigned int cnt[kPwFootMax];
     int wsum[40];
-    int wi0, wi1, wj0, wj1, Wc, Hc, hw;         // the window: cells [wi0, wi1] x [wj0, wj1], hw words per column
+    int wi0, wi1, wj0, wj1, Wc, Hc, hw, hs;     // the window: cells [wi0, wi1] x [wj0, wj1], hw words per
+                                                // column stored hs = sparse_col_stride(hw) words apart
     int fx0, fx1, fy0, fy1, nsamples;           // owned-pixel footprint, owned samples
     int rw_min, rw_max, rh_min, rh_max;         // extremes of the offsets' rectangle widths and heights
-    int stop;
+    int stop, ngrains;
     float est_grains, est_cells;
 };
 
@@ -116,34 +136,40 @@ __device__ __forceinline__ void sparse_defer(const PixelwiseArgs &a, const PwSpa
     }
 }
 
-// Sample (xg, yg): 0 not covered, 1 covered, 2 its cell range leaves the window (the per-sample loop
-// decides it, in a second pass).  The reference's cell range (src/pixelwise.rs:55-58), one 64-bit
-// shared load per cell column for the bits of rows j0..j1, the disk test on the grains of the set bits
-// (src/pixelwise.rs:96-99).
-__device__ __forceinline__ int sparse_sample_hit(const PixelwiseArgs &a, const PwSparseShared &S, float xg, float yg,
-                                                 int j0, int j1) {
-    if (!(a.rm > 0.0f)) return 0;
-    const int i0 = f2i_floor(FG_FDIV(FG_FSUB(xg, a.rm), a.delta));
-    const int i1 = f2i_floor(FG_FDIV(FG_FADD(xg, a.rm), a.delta));
-    if (i0 > i1 || j0 > j1) return 0;  // no cell (src/pixelwise.rs:60-62)
-    const int wi0 = S.wi0, wj0 = S.wj0, hw = S.hw;
-    const unsigned span = (unsigned)(j1 - j0);
-    if (i0 < wi0 || i1 > S.wi1 || j0 < wj0 || j1 > S.wj1 || span >= 32u) return 2;
-    const int r0 = j0 - wj0, b0 = r0 & 31;
-    const unsigned keep = (2u << span) - 1u;  // span <= 31: 2u << 31 wraps to 0 and keep is all ones
+// Sample (xg, yg) with cell-range codes rx, ry (neither kRangeSlow): 1 covered, else 0.  For each cell
+// column of the range (src/pixelwise.rs:55-58) one 64-bit shared load gives the bits of its rows; the
+// grains of the non-empty cells get the disk test (src/pixelwise.rs:96-99).  The columns are scanned
+// first, branch-free, into a mask of the ones holding non-empty cells, and only those are visited: a
+// warp's lanes then diverge over their few non-empty columns instead of over every column.
+__device__ __forceinline__ int sparse_sample_hit(const PwSparseShared &S, float xg, float yg, unsigned rx,
+                                                 unsigned ry) {
+    const int hs = S.hs;
+    const int c0 = (int)(rx & 0x7FFu), ncol = (int)(rx >> 11);
+    const int r0 = (int)(ry & 0x7FFu), b0 = r0 & 31;
+    const unsigned keep = (2u << (ry >> 11)) - 1u;  // span <= 31: 2u << 31 wraps to 0 and keep is all ones
     const unsigned below = (1u << b0) - 1u;
-    int w = (i0 - wi0) * hw + (r0 >> 5);
-    for (int i = i0; i <= i1; i++, w += hw) {
+    const int w0 = c0 * hs + (r0 >> 5);
+    unsigned cols = 0u;
+    for (int i = 0; i <= ncol; i++) {
+        const uint2 m = S.mask2[w0 + i * hs];
+        cols |= ((__funnelshift_r(m.x, m.y, b0) & keep) != 0u ? 1u : 0u) << i;
+    }
+    while (cols) {
+        const int w = w0 + (__ffs(cols) - 1) * hs;
+        cols &= cols - 1u;
         const uint2 m = S.mask2[w];
-        const unsigned bits = __funnelshift_r(m.x, m.y, b0) & keep;
-        if (!bits) continue;
-        const int rank = S.wrank[w] + __popc(m.x & below);
-        const int ge = S.gstart[rank + __popc(bits)];
-        for (int g = S.gstart[rank]; g < ge; g++) {
-            const float4 G = S.grains[g];
-            const float dx = FG_FSUB(xg, G.x), dy = FG_FSUB(yg, G.y);
-            if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= G.z) return 1;
-        }
+        unsigned bits = __funnelshift_r(m.x, m.y, b0) & keep;
+        int rank = S.wrank[w] + __popc(m.x & below);
+        do {  // the column's non-empty cells of the range, in row order
+            bits &= bits - 1u;
+            const unsigned sc = S.gsc[rank++];
+            const int g0 = (int)(sc & 0xFFFFu), ge = g0 + (int)(sc >> 16);
+            for (int g = g0; g < ge; g++) {
+                const float4 G = S.grains[g];
+                const float dx = FG_FSUB(xg, G.x), dy = FG_FSUB(yg, G.y);
+                if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= G.z) return 1;
+            }
+        } while (bits);
     }
     return 0;
 }
@@ -160,57 +186,39 @@ __device__ __forceinline__ void sparse_count_hit(const PixelwiseArgs &a, PwSpars
         atomicAdd(&a.out[(long long)y * a.out_w + x], 1.0f);
 }
 
-// Step 3, out of line (its loops get the whole register budget).  When every offset owns a
-// rectangle of the same power-of-two size (zoom 1 away from the plane's edges), consecutive threads
-// take consecutive pixels of one offset -- neighbouring samples, similar cell ranges; otherwise each
-// thread takes the pixels of one offset (`parts` threads per offset when N < the CTA size).
+// Step 3.  The offsets are sorted by x, and consecutive threads take consecutive offsets, each walking
+// the pixels its offset owns (`parts` threads per offset, taking alternate rows, when N < the CTA
+// size): a warp's lanes evaluate samples of about the same pixel whose points lie close together in x,
+// so their mask loads fall on neighbouring columns.  Cell ranges come from the table the ownership pass
+// filled when every rectangle fits it, else they are computed here.
 // One pass over the thread's samples: pass 0 evaluates every sample from the staged window and counts
 // the ones whose range leaves it; pass 1 sends exactly those to the per-sample loop.
 template <int kPass>
 __device__ __forceinline__ unsigned sparse_sample_pass(const PixelwiseArgs &a, PwSparseShared &S) {
+    using C = PwSparse;
     const int tid = threadIdx.x, nthreads = blockDim.x;
     unsigned slow = 0;
-    const int W = S.rw_min, H = S.rh_min;
-    const bool uniform = W == S.rw_max && H == S.rh_max && W > 0 && H > 0 && (W & (W - 1)) == 0 &&
-                         (H & (H - 1)) == 0 && W * H <= 1024;
-    if (uniform) {
-        const int lw = __ffs(W) - 1, lp = lw + __ffs(H) - 1;
-        const int total = a.n << lp;
-        for (int s = tid; s < total; s += nthreads) {
-            const int k = s >> lp, pix = s & ((1 << lp) - 1);
-            const int4 R = S.rect[k];
-            const float2 o = a.offs[k];
-            const int x = R.x + (pix & (W - 1)), y = R.z + (pix >> lw);
-            const float xg = xg_of(x, a.inv_zoom, o.x), yg = xg_of(y, a.inv_zoom, o.y);
-            const int j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
-            const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
-            const int h = sparse_sample_hit(a, S, xg, yg, j0, j1);
-            if (kPass == 0) {
-                if (h == 1) sparse_count_hit(a, S, x, y);
-                slow += h == 2;
-            } else if (h == 2) {
-                sparse_slow_sample(a, S, xg, yg, x, y);
-            }
-        }
-    } else {
-        const int parts = a.n >= nthreads ? 1 : nthreads / a.n;
-        for (int t = tid; t < a.n * parts; t += nthreads) {
-            const int k = t / parts, p = t % parts;
-            const int4 R = S.rect[k];
-            const float2 o = a.offs[k];
-            for (int y = R.z + p; y < R.w; y += parts) {
-                const float yg = xg_of(y, a.inv_zoom, o.y);
-                const int j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
-                const int j1 = f2i_floor(FG_FDIV(FG_FADD(yg, a.rm), a.delta));
-                for (int x = R.x; x < R.y; x++) {
-                    const float xg = xg_of(x, a.inv_zoom, o.x);
-                    const int h = sparse_sample_hit(a, S, xg, yg, j0, j1);
-                    if (kPass == 0) {
-                        if (h == 1) sparse_count_hit(a, S, x, y);
-                        slow += h == 2;
-                    } else if (h == 2) {
-                        sparse_slow_sample(a, S, xg, yg, x, y);
-                    }
+    const bool table = S.rw_max <= C::kRangeSlots && S.rh_max <= C::kRangeSlots;
+    const int parts = a.n >= nthreads ? 1 : nthreads / a.n;
+    const int wi0 = S.wi0, wi1 = S.wi1, wj0 = S.wj0, wj1 = S.wj1;
+    for (int t = tid; t < a.n * parts; t += nthreads) {
+        const int k = t % a.n, p = t / a.n;
+        const int4 R = S.rect[k];
+        const float2 o = a.offs[k];
+        for (int y = R.z + p; y < R.w; y += parts) {
+            const float yg = xg_of(y, a.inv_zoom, o.y);
+            const unsigned ry = table ? S.range_y[(y - R.z) * a.n + k]
+                                      : sparse_range_code(yg, a.rm, a.delta, wj0, wj1);
+            for (int x = R.x; x < R.y; x++) {
+                const float xg = xg_of(x, a.inv_zoom, o.x);
+                const unsigned rx = table ? S.range_x[(x - R.x) * a.n + k]
+                                          : sparse_range_code(xg, a.rm, a.delta, wi0, wi1);
+                const bool out = rx == kRangeSlow || ry == kRangeSlow;
+                if (kPass == 0) {
+                    if (out) slow++;
+                    else if (sparse_sample_hit(S, xg, yg, rx, ry)) sparse_count_hit(a, S, x, y);
+                } else if (out) {
+                    sparse_slow_sample(a, S, xg, yg, x, y);
                 }
             }
         }
@@ -219,6 +227,7 @@ __device__ __forceinline__ unsigned sparse_sample_pass(const PixelwiseArgs &a, P
 }
 
 __device__ __noinline__ void sparse_samples(const PixelwiseArgs &a, PwSparseShared &S) {
+    if (!(a.rm > 0.0f)) return;  // a grain radius is at most rm: nothing can cover a sample
     const unsigned slow = sparse_sample_pass<0>(a, S);
     if (__syncthreads_or(slow != 0)) {
         if (slow) atomicAdd(&a.diag[0], (unsigned long long)slow);
@@ -240,9 +249,10 @@ __device__ __noinline__ void sparse_slow_sample(const PixelwiseArgs &a, PwSparse
 // the grains overflow their shared-memory buffers.
 __device__ __noinline__ bool sparse_stage(const PixelwiseArgs &a, PwSparseShared &S) {
     using C = PwSparse;
-    const int tid = threadIdx.x, nthreads = blockDim.x;
-    const int Wc = S.Wc, Hc = S.Hc, hw = S.hw, wi0 = S.wi0, wj0 = S.wj0;
-    const int nwords = Wc * hw;
+    const int tid = threadIdx.x, nthreads = blockDim.x, lane = tid & 31;
+    const int Wc = S.Wc, Hc = S.Hc, hs = S.hs, wi0 = S.wi0, wj0 = S.wj0;
+    if (tid == 0) S.ngrains = 0;  // read after the list's barrier
+    const int nwords = Wc * hs;
     int nlist;
     {
         const int per = (nwords + nthreads - 1) / nthreads;
@@ -256,7 +266,7 @@ __device__ __noinline__ bool sparse_stage(const PixelwiseArgs &a, PwSparseShared
             for (int w = b; w < e; w++) {
                 S.wrank[w] = (unsigned short)run;
                 unsigned m = S.mask2[w].x;
-                const int col = w / hw, row0 = (w - col * hw) * 32;
+                const int col = w / hs, row0 = (w - col * hs) * 32;
                 while (m) {
                     const int bit = __ffs(m) - 1;
                     m &= m - 1u;
@@ -267,60 +277,50 @@ __device__ __noinline__ bool sparse_stage(const PixelwiseArgs &a, PwSparseShared
     }
     __syncthreads();
     if (nlist > C::kListMax) return false;
-    for (int t = tid; t < nlist; t += nthreads) {
-        const int c = S.list[t];
-        Xoshiro rng;
-        const uint32_t q = sparse_cell_count(a, wi0 + c / Hc, wj0 + c % Hc, &rng);
-        S.gstart[t] = (unsigned short)(q > 65535u ? 65535u : q);
-    }
-    __syncthreads();
-    int ngrains;
-    {
-        const int per = (nlist + nthreads - 1) / nthreads;
-        const int b = tid * per, e = min(nlist, b + per);
-        int local = 0;
-        for (int t = b; t < e; t++) local += S.gstart[t];
-        int total;
-        int run = block_excl_scan(local, S.wsum, &total);
-        ngrains = total;
-        if (total <= C::kGrainMax) {
-            for (int t = b; t < e; t++) {
-                const int q = S.gstart[t];
-                S.gstart[t] = (unsigned short)run;
-                run += q;
-            }
-            if (tid == 0) S.gstart[nlist] = (unsigned short)total;
-        }
-    }
-    __syncthreads();
-    if (ngrains > C::kGrainMax) return false;
+    // counts and grains in one pass: a warp takes 32 consecutive listed cells at a time, each lane counts
+    // its cell's grains (the Poisson draws of src/pixelwise.rs:77-82), the lanes reserve their grains'
+    // slots with a warp scan and one shared counter, and each lane regenerates its grains from the
+    // stream the Poisson draws left (src/pixelwise.rs:84-95)
     const UniformF32 U = uniform_f32_new(0.0f, a.delta);
-    for (int t = tid; t < nlist; t += nthreads) {
-        const int c = S.list[t];
-        const int i = wi0 + c / Hc, j = wj0 + c % Hc;
-        const CellParam cp = a.cells[cell_pixel(a, i, j)];
-        const int base = S.gstart[t];
-        uint32_t q = (uint32_t)(S.gstart[t + 1] - base);
+    for (int t0 = tid & ~31; t0 < nlist; t0 += nthreads) {  // warp-uniform bounds (the shuffles below)
+        const int t = t0 + lane;
+        int i = 0, j = 0;
+        uint32_t q = 0u;
         Xoshiro rng;
-        if (cp.thresh >= 0) {
-            // Knuth regime: the Poisson draw consumed exactly q + 1 uniforms; skip them.
-            rng = small_seed(cell_row_hash(cell_col_hash(a.seed, i), j));
-            for (uint32_t k = 0; k <= q; k++) (void)rng.next();
-        } else {
-            q = min(q, sparse_cell_count(a, i, j, &rng));
+        if (t < nlist) {
+            const int c = S.list[t];
+            i = wi0 + c / Hc;
+            j = wj0 + c % Hc;
+            q = sparse_cell_count(a, i, j, &rng);
         }
-        const float sx = FG_FMUL((float)i, a.delta), sy = FG_FMUL((float)j, a.delta);
-        for (uint32_t k = 0; k < q; k++) {
-            const float cx = FG_FADD(sx, uniform_f32_from(U, rng.next()));
-            const float cy = FG_FADD(sy, uniform_f32_from(U, rng.next()));
-            float r = radius_draw(a, rng);
-            if (r > a.rm) r = a.rm;
-            const float rr = (r <= 0.0f) ? -1.0f : FG_FMUL(r, r);  // -1 never passes the disk test
-            S.grains[base + k] = make_float4(cx, cy, rr, 0.0f);
+        const int qc = (int)min(q, (uint32_t)C::kGrainMax + 1u);
+        int incl = qc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        int base = 0;
+        if (lane == 31) base = atomicAdd(&S.ngrains, incl);  // lane 31 holds the warp's total
+        base = __shfl_sync(0xffffffffu, base, 31);
+        const int first = base + incl - qc;
+        if (t < nlist) {
+            S.gsc[t] = (unsigned)(first & 0xFFFF) | ((unsigned)min(qc, 0xFFFF) << 16);
+            if (first + qc <= C::kGrainMax) {
+                const float sx = FG_FMUL((float)i, a.delta), sy = FG_FMUL((float)j, a.delta);
+                for (int k = 0; k < qc; k++) {
+                    const float cx = FG_FADD(sx, uniform_f32_from(U, rng.next()));
+                    const float cy = FG_FADD(sy, uniform_f32_from(U, rng.next()));
+                    float r = radius_draw(a, rng);
+                    if (r > a.rm) r = a.rm;
+                    const float rr = (r <= 0.0f) ? -1.0f : FG_FMUL(r, r);  // -1 never passes the disk test
+                    S.grains[first + k] = make_float4(cx, cy, rr, 0.0f);
+                }
+            }
         }
     }
     __syncthreads();
-    return true;
+    return S.ngrains <= C::kGrainMax;  // an overflow wrote no grain past the buffer; the block is redone
 }
 
 // One block of edge bs at block coordinates (bx, by) (all threads of the CTA; `smem_raw` holds
@@ -345,11 +345,12 @@ __device__ __noinline__ int pixelwise_sparse_block(const PixelwiseArgs &a, const
     const int wj1 = f2i_floor(FG_FDIV(FG_FADD(Y1, a.rm), a.delta));
     const int Wc = wi1 - wi0 + 1, Hc = wj1 - wj0 + 1;
     const int hw = (Hc + 31) >> 5;  // mask words per window column
-    const bool fits = Wc > 0 && Hc > 0 && Hc <= C::kRowsMax && Wc * hw <= C::kMaskWords &&
+    const int hs = sparse_col_stride(hw);
+    const bool fits = Wc > 0 && Hc > 0 && Hc <= C::kRowsMax && Wc * hs <= C::kMaskWords &&
                       wi0 >= g.gi0 && wi1 < g.gi0 + g.gw && wj0 >= g.gj0 && wj1 < g.gj0 + 32 * (g.ghw - 1);
 
     if (tid == 0) {
-        S.wi0 = wi0; S.wi1 = wi1; S.wj0 = wj0; S.wj1 = wj1; S.Wc = Wc; S.Hc = Hc; S.hw = hw;
+        S.wi0 = wi0; S.wi1 = wi1; S.wj0 = wj0; S.wj1 = wj1; S.Wc = Wc; S.Hc = Hc; S.hw = hw; S.hs = hs;
         S.est_grains = 0.0f;
         S.est_cells = 0.0f;
         S.fx0 = 0x7fffffff; S.fx1 = -1; S.fy0 = 0x7fffffff; S.fy1 = -1; S.nsamples = 0;
@@ -398,6 +399,13 @@ __device__ __noinline__ int pixelwise_sparse_block(const PixelwiseArgs &a, const
             const int ya = first_at_least(Y0, a.out_h, a.inv_zoom, a.zoom, o.y);
             const int ye = first_at_least(Y1, a.out_h, a.inv_zoom, a.zoom, o.y);
             S.rect[k] = make_int4(xa, xe, ya, ye);
+            // the cell ranges of the rectangle's first columns and rows (pixelwise_sparse_block's table)
+            for (int s2 = 0; s2 < min(xe - xa, C::kRangeSlots); s2++)
+                S.range_x[s2 * a.n + k] =
+                    (unsigned short)sparse_range_code(xg_of(xa + s2, a.inv_zoom, o.x), a.rm, a.delta, wi0, wi1);
+            for (int s2 = 0; s2 < min(ye - ya, C::kRangeSlots); s2++)
+                S.range_y[s2 * a.n + k] =
+                    (unsigned short)sparse_range_code(xg_of(ya + s2, a.inv_zoom, o.y), a.rm, a.delta, wj0, wj1);
             wmin = min(wmin, xe - xa); wmax = max(wmax, xe - xa);
             hmin = min(hmin, ye - ya); hmax = max(hmax, ye - ya);
             if (xe > xa && ye > ya) {
@@ -445,18 +453,21 @@ __device__ __noinline__ int pixelwise_sparse_block(const PixelwiseArgs &a, const
     {
         const int rb = wj0 - g.gj0, rw = rb >> 5, rs = rb & 31;
         const unsigned tail = (Hc & 31) ? ((1u << (Hc & 31)) - 1u) : 0xffffffffu;
-        for (int idx = tid; idx < Wc * hw; idx += nthreads) {
+        for (int idx = tid; idx < Wc * hs; idx += nthreads) {
             const int k = idx / Wc, c = idx - k * Wc;  // consecutive threads: consecutive columns
-            const int gc = wi0 - g.gi0 + c;
-            const unsigned lo = g.cellmask[(long long)(rw + k) * g.gw + gc];
-            const unsigned hi = rs ? g.cellmask[(long long)(rw + k + 1) * g.gw + gc] : 0u;
-            unsigned word = __funnelshift_r(lo, hi, rs);
-            if (k == hw - 1) word &= tail;
-            S.mask2[c * hw + k].x = word;
+            unsigned word = 0u;                        // the pad word of an even hw stays empty
+            if (k < hw) {
+                const int gc = wi0 - g.gi0 + c;
+                const unsigned lo = g.cellmask[(long long)(rw + k) * g.gw + gc];
+                const unsigned hi = rs ? g.cellmask[(long long)(rw + k + 1) * g.gw + gc] : 0u;
+                word = __funnelshift_r(lo, hi, rs);
+                if (k == hw - 1) word &= tail;
+            }
+            S.mask2[c * hs + k].x = word;
         }
         __syncthreads();
-        for (int w = tid; w < Wc * hw; w += nthreads) {
-            const int k = w % hw;
+        for (int w = tid; w < Wc * hs; w += nthreads) {
+            const int k = w % hs;
             S.mask2[w].y = k + 1 < hw ? S.mask2[w + 1].x : 0u;
         }
         __syncthreads();

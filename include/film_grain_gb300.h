@@ -329,8 +329,9 @@ FG_API const char *fg_last_error_message(void);
  * shared-memory overflow, [3] blocks processed.  No counterpart in the crate (diagnostics only). */
 FG_API void fg_pixelwise_diagnostics(unsigned long long out[4]);
 /* Kernel launches one pixel-wise render of these params makes: 3 when the plane takes the per-sample
- * kernel (cell table, per-sample kernel, epilogue), 5 when it takes the sparse block pass (cell table,
- * the plane's cell-emptiness bitmask, sparse and fat block passes, epilogue), 4 when it takes the
+ * kernel (cell table, per-sample kernel, epilogue), 6 when it takes the sparse block pass (cell table,
+ * the plane's cell-emptiness bitmask, the offsets sorted by x, sparse and fat block passes, epilogue),
+ * 4 when it takes the
  * lean block pass (cell table, lean and fat block passes, epilogue).  offsets_input as for
  * fg_render_pixelwise.  No counterpart in the crate (diagnostics only). */
 FG_API fg_status fg_pixelwise_kernel_count(const fg_params *params, const fg_derived *derived,

@@ -65,8 +65,8 @@ def test_choose_algorithm_rules(fgl):
 
 def test_pixelwise_kernel_choice(fgl):
     """The plane-level choice between the per-sample kernel (3 launches per plane) and the block
-    kernels (5: the cell table, the plane's emptiness bitmask, the sparse and fat block passes, the
-    epilogue): an interior root block's samples x the cells of one sample's range, against 1.5 x the
+    kernels (6: the cell table, the plane's emptiness bitmask, the offsets sorted by x, the sparse and
+    fat block passes, the epilogue): an interior root block's samples x the cells of one sample's range, against 1.5 x the
     cells of its staged window."""
     def kernels(**kw):
         p = fgl.ParamsBuilder(algo=fgl.Algo.Pixel, **kw).build()
@@ -75,15 +75,15 @@ def test_pixelwise_kernel_choice(fgl):
     assert kernels(radius_mean=0.025, n_samples=64) == 3      # 0.34
     assert kernels(radius_mean=0.05, n_samples=64) == 3       # 1.37
     assert kernels(radius_mean=0.025, n_samples=256) == 3     # 1.37
-    assert kernels(radius_mean=0.05, n_samples=256) == 5      # 5.5
-    assert kernels(radius_mean=0.1, n_samples=64) == 5        # 5.5
-    assert kernels(radius_mean=0.12, n_samples=64) == 5       # the 256^2 luma workload, 7.3
+    assert kernels(radius_mean=0.05, n_samples=256) == 6      # 5.5
+    assert kernels(radius_mean=0.1, n_samples=64) == 6        # 5.5
+    assert kernels(radius_mean=0.12, n_samples=64) == 6       # the 256^2 luma workload, 7.3
     assert kernels(radius_mean=0.025, radius_dist=fgl.RadiusDist.Lognorm, radius_stddev=0.01,
-                   n_samples=256) == 5                        # the 4096^2 frame's parameters, 6.8
+                   n_samples=256) == 6                        # the 4096^2 frame's parameters, 6.8
     assert kernels(radius_mean=0.05, radius_dist=fgl.RadiusDist.Lognorm, radius_stddev=0.02, n_samples=2,
                    zoom=2.0) == 3                             # a 64-cell range: the widest the kernel takes
     # a range wider than the per-sample kernel's 64-cell mask stays on the block kernels
-    assert kernels(radius_mean=0.3, n_samples=1, cell_delta=0.05) == 5
+    assert kernels(radius_mean=0.3, n_samples=1, cell_delta=0.05) == 6
 
 
 def test_lambda_and_normalize_match_oracle(fgl, orc):
