@@ -293,7 +293,10 @@ def surrogate_compare(fg, sg, net, steps, warmup, plain_steps, clocks=None, seed
     planes = host_planes(workloads.blobs_rgb(size, size, wl["image_seed"]), "rgb")
     u_host = np.stack([fg.normalize_plane(p)[0] for p in planes])
     u_dev = torch.from_numpy(u_host).cuda()
-    radius = torch.full((3,), wl["radius"], dtype=torch.float32, device="cuda")
+    # the lognormal radius as the constant radius of equal grain power (the network's training radii are
+    # constant)
+    radius = torch.full((3,), sg.grain_radius(wl["radius"], wl["sd"], lognormal=True), dtype=torch.float32,
+                        device="cuda")
     y = torch.empty_like(u_dev)
     L = fg.lib()
     stream = torch.cuda.current_stream()
@@ -364,6 +367,15 @@ def surrogate_compare(fg, sg, net, steps, warmup, plain_steps, clocks=None, seed
     q_plain = sg.evaluate(plain256, ref1024)
     q_eq = dict(sg.evaluate(plain_eq, ref1024), n_samples=n_eq)
     q_id = sg.evaluate(u_dev, ref1024)
+    # the same network with its noise input off predicts the expectation instead of a grain realisation
+    y_mean = net.infer(u_dev, radius, seed=seed, grain=False)
+    q_mean = sg.evaluate(y_mean, ref1024)
+    # grain-band spectrum error (radial bins up to 0.25 cycles/px of each render's residual against the
+    # expectation, Monte Carlo floors of plain renders removed) against the N=1024 render
+    grain_band = {"surrogate": sg.grain_band_error(y, ref1024, u_dev, None, 1024),
+                  "surrogate_no_noise": sg.grain_band_error(y_mean, ref1024, u_dev, None, 1024),
+                  "identity": sg.grain_band_error(u_dev, ref1024, u_dev, None, 1024),
+                  "plain_n256": sg.grain_band_error(plain256, ref1024, u_dev, 256, 1024)}
 
     # end to end: pinned host u planes in, pinned host f32 planes out
     pin_u = torch.from_numpy(u_host).pin_memory()
@@ -383,7 +395,8 @@ def surrogate_compare(fg, sg, net, steps, warmup, plain_steps, clocks=None, seed
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) / steps * 1e3
     return dict(size=size, sur_ms=sur_ms, plain_ms=plain_ms, conv_ms=conv_ms, conv_flop=conv_flop,
-                conv_bytes=conv_bytes, q_sur=q_sur, q_plain=q_plain, q_eq=q_eq, q_id=q_id, e2e_ms=e2e_ms,
+                conv_bytes=conv_bytes, q_sur=q_sur, q_plain=q_plain, q_eq=q_eq, q_id=q_id, q_mean=q_mean,
+                grain_band=grain_band, e2e_ms=e2e_ms,
                 h2d=4 * px, d2h=4 * px, clocks=clk, launches_per_frame=3 + net.n_res, wl=wl, planes=planes)
 
 
@@ -414,6 +427,8 @@ def surrogate_line(steps, warmup, world, retrain=False, cpu=True):
                        "l2": "256 MiB flush write before every frame", "network": prov},
             "quality": {"surrogate_vs_n1024": r["q_sur"], "plain_n256_vs_n1024": r["q_plain"],
                         "plain_equal_time_vs_n1024": r["q_eq"], "identity_vs_n1024": r["q_id"],
+                        "surrogate_no_noise_vs_n1024": r["q_mean"],
+                        "grain_band_error_vs_n1024": r["grain_band"],
                         "targets": {"mae": 0.01, "raps": 0.02}},
             "roofline": {"bound": "tensor", "achieved": ach, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                          "frac": ach / peaks["bf16_tflops"],

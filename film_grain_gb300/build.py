@@ -23,7 +23,7 @@ ROOT = os.path.dirname(HERE)
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_EXACT = ["fg_pixelwise.cu", "fg_grainwise.cu", "fg_capi.cu", "fg_noalloc.cu", "fg_batch.cu", "fg_lambda.cu"]
-CU_FAST = ["fg_surrogate.cu"]
+CU_FAST = ["fg_surrogate.cu", "fg_sg_tc.cu"]
 CPP = ["fg_host.cpp"]
 
 NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",

@@ -464,6 +464,11 @@ static cudaError_t launch_conv_t(const SgConvArgs &a, int total, cudaStream_t s)
     return cudaGetLastError();
 }
 
+// fg_sg_tc.cu: the residual conv on the tcgen05 tensor cores (TMA-staged rows, accumulator in tensor
+// memory); cudaErrorNotSupported when its preconditions fail.
+cudaError_t launch_sg_conv32_tc(const void *in, const void *w, const float *bias, void *out, void *aux, int nb, int H,
+                                int W, cudaStream_t s);
+
 static fg_status launch_conv(int32_t kind, const SgConvArgs &a, int nb, cudaStream_t s) {
     const long long blocks = (long long)nb * a.tiles_per_img;
     if (blocks > 0x7FFFFFFFll) return set_error(FG_ERR_UNSUPPORTED, "surrogate batch too large");
@@ -471,7 +476,16 @@ static fg_status launch_conv(int32_t kind, const SgConvArgs &a, int nb, cudaStre
     cudaError_t e;
     switch (kind) {
     case FG_SG_CONV_INPUT: e = launch_conv_t<16, 32, kSgRelu>(a, total, s); break;
-    case FG_SG_CONV_RESIDUAL: e = launch_conv_t<32, 32, kSgResidual>(a, total, s); break;
+    case FG_SG_CONV_RESIDUAL:
+        // the residual is the conv's own input (every residual layer of the network): tensor cores
+        e = a.res == a.in && a.in_cstride == 32
+                ? launch_sg_conv32_tc(a.in, a.w, a.bias, a.out, a.aux, nb, a.H, a.W, s)
+                : cudaErrorNotSupported;
+        if (e == cudaErrorNotSupported) {
+            cudaGetLastError();
+            e = launch_conv_t<32, 32, kSgResidual>(a, total, s);
+        }
+        break;
     case FG_SG_CONV_OUTPUT: e = launch_conv_t<32, 8, kSgOutput>(a, total, s); break;
     case FG_SG_CONV_DGRAD_RESIDUAL: e = launch_conv_t<32, 32, kSgLinearAdd>(a, total, s); break;
     case FG_SG_CONV_DGRAD_OUTPUT: e = launch_conv_t<16, 32, kSgLinear>(a, total, s); break;

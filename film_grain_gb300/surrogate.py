@@ -10,6 +10,17 @@ Network (every conv 3x3, zero padding; weights bf16 on the tensor cores, f32 acc
 Forward, backward and the Adam step run in the library's own kernels (include/film_grain_gb300.h,
 fg_sg_*); this module owns the parameter buffers and sequences the launches.  Parameters live in one
 flat f32 vector (the master copy Adam updates) mirrored by a flat bf16 vector the kernels read.
+
+Grain.  A plain render is its expectation (u under the sample filter) plus the film grain of its grain
+realisation (low frequencies: the coverage field seen through the Gaussian filter) plus the
+integrator's Monte Carlo error (white, variance f(1 - f)/N per pixel).  The network renders a grain
+realisation of its own from the noise input: it is trained on pairs of outputs for the same tile and
+two noise fields, with a mean-square term that is blind to the noise part (the paired form
+E(m - t)^2 - E d^2 / 2, m the pair's mean, d its half-difference / sqrt 2) and a spectral term that
+matches the radial power of d to the grain power of the target (its residual against the expectation,
+less the Monte Carlo floor).  A third pass with the noise channel's input weights zeroed is trained on
+plain mean-square error, so that the same network with those weights zeroed predicts the expectation
+instead (`grain=False`).
 """
 from __future__ import annotations
 
@@ -27,7 +38,8 @@ CH = 32          # residual stream channels
 CH_IN = 16       # padded input channels (3 used)
 CH_OUT = 8       # computed output channels (1 used)
 N_INPUTS = 3
-NOISE_WEIGHT_DECAY = 100.0  # per-step shrink 1 - lr * 100 of the noise channel's input weights
+NOISE_CHANNEL = 1
+GRAIN_FMAX = 0.75  # the spectral training term covers every radial bin of a tile (the corners reach 0.71)
 
 
 def _layout(n_res: int):
@@ -69,12 +81,7 @@ class SurrogateNet:
         self.v = torch.zeros_like(self.w32)
         self.grad = torch.zeros_like(self.w32)
         self.ema = self.w32.clone()  # exponential moving average of the weights (what inference ships)
-        # Decoupled weight decay per parameter: only the noise channel's input weights.  Under the MSE
-        # objective the optimal output does not depend on the noise, but Adam turns their zero-mean
-        # gradients into a random walk of step ~lr; the decay holds them near zero.
-        dec = np.zeros(self.n_params, np.float32)
-        self._np_view(dec, "w_in")[:, :, 1] = NOISE_WEIGHT_DECAY
-        self.decay = torch.from_numpy(dec).to(self.device)
+        self.decay = torch.zeros_like(self.w32)  # decoupled weight decay per parameter (none)
         self._ws: Dict[Tuple[int, int, int], dict] = {}
         self._wt_res = torch.zeros(CH * 9 * CH, dtype=torch.bfloat16, device=self.device)
         self._wt_out = torch.zeros(CH * 9 * CH_IN, dtype=torch.bfloat16, device=self.device)
@@ -156,7 +163,9 @@ class SurrogateNet:
                           dh=torch.empty((nb, h, w, CH), dtype=bf, device=dev),
                           dz=torch.empty((nb, h, w, CH), dtype=bf, device=dev),
                           loss=torch.zeros(1, dtype=torch.float32, device=dev))
-            self._ws = {k: v for k, v in self._ws.items() if k[3] != train}  # one shape per mode stays resident
+            same_mode = [k for k in self._ws if k[3] == train]
+            if len(same_mode) >= 2:  # two shapes per mode stay resident (grain training uses two)
+                del self._ws[same_mode[0]]
             self._ws[key] = ws
         return ws
 
@@ -191,13 +200,28 @@ class SurrogateNet:
         last forward(keep=True).  Returns the device loss-sum tensor (sum of squared errors)."""
         nb, h, w = u.shape
         ws = self._workspace(nb, h, w)
-        L, s = lib(), _stream()
         n = nb * h * w
-        self.grad.zero_()
         ws["loss"].zero_()
+        _raise(lib().fg_sg_mse_grad(ws["y"].data_ptr(), target.data_ptr(), ws["dy"].data_ptr(), ws["loss"].data_ptr(),
+                                    n, 2.0 / n, _stream()))
+        self._backward_layers(ws, nb, h, w)
+        return ws["loss"]
+
+    def backward_from(self, dy):
+        """Gradients into self.grad (zeroed first) for a loss whose gradient with respect to the output
+        of the last forward(keep=True) is dy [nb, h, w] f32."""
+        import torch
+        nb, h, w = dy.shape
+        ws = self._workspace(nb, h, w)
+        ws["dy"].zero_()
+        ws["dy"][..., 0] = dy.to(torch.bfloat16)
+        self._backward_layers(ws, nb, h, w)
+
+    def _backward_layers(self, ws, nb, h, w):
+        """The backward pass through every layer from the output gradient in ws["dy"]."""
+        L, s = lib(), _stream()
+        self.grad.zero_()
         g = self.grad
-        _raise(L.fg_sg_mse_grad(ws["y"].data_ptr(), target.data_ptr(), ws["dy"].data_ptr(), ws["loss"].data_ptr(), n,
-                                2.0 / n, s))
         hs, rs = ws["hs"], ws["rs"]
         _raise(L.fg_sg_conv_wgrad(CONV_OUTPUT, ws["dy"].data_ptr(), CH_IN, hs[self.n_res].data_ptr(), CH,
                                   self._ptr(g, "w_out"), self._ptr(g, "b_out"), nb, h, w, s))
@@ -214,7 +238,6 @@ class SurrogateNet:
         _raise(L.fg_sg_mask_grad(dh.data_ptr(), hs[0].data_ptr(), dz.data_ptr(), dz.numel(), s))
         _raise(L.fg_sg_conv_wgrad(CONV_INPUT, dz.data_ptr(), CH, ws["x"].data_ptr(), CH_IN, self._ptr(g, "w_in"),
                                   self._ptr(g, "b_in"), nb, h, w, s))
-        return ws["loss"]
 
     def adam_step(self, lr: float = 1e-3, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8,
                   ema_decay: float = 0.999):
@@ -226,11 +249,50 @@ class SurrogateNet:
                                 beta1, beta2, eps, self.step, _stream()))
 
     def train_step(self, u, radius, target, seed: int, lr: float = 1e-3, ema_decay: float = 0.999):
-        """One Adam step on a batch; returns the device loss-sum tensor (read it only when needed)."""
+        """One Adam step on a batch under mean((y - target)^2); returns the device loss-sum tensor (read
+        it only when needed)."""
         self.forward(u, radius, seed, keep=True)
         loss = self.backward(u, target)
         self.adam_step(lr, ema_decay=ema_decay)
         return loss
+
+    def train_step_grain(self, u, radius, target, seed: int, n_target: int, lr: float = 1e-3,
+                         ema_decay: float = 0.999, spec_weight: float = 0.01):
+        """One Adam step of grain training on a batch of tiles (see the module docstring): the network runs
+        on every tile twice, with two noise fields, and the loss is the paired mean-square term plus
+        spec_weight x the spectral term: per radial bin, the mean square difference between the pairs'
+        noise-part power and the targets' grain power (target renders at n_target samples), relative to
+        the bin's mean grain power plus the Monte Carlo floor -- so power the network adds where the
+        targets have no grain (high frequencies) costs as much as power missing where they have it.  A
+        third pass, with the noise channel's input weights zeroed, adds the plain mean-square error of
+        that network (the expectation predictor; the zeroed weights get no gradient from it).
+        Returns (paired MSE, spectral term) tensors."""
+        import torch
+        nb, h, w = u.shape
+        # the expectation pass first: its gradients are kept while the pairs' pass reuses self.grad
+        noise_w = self.view(self.wbf, "w_in")[:, :, NOISE_CHANNEL]
+        kept = noise_w.clone()
+        noise_w.zero_()
+        self.forward(u, radius, seed ^ 0x5DEECE66D, keep=True)
+        self.backward(u, target)
+        noise_w.copy_(kept)
+        self.view(self.grad, "w_in")[:, :, NOISE_CHANNEL] = 0.0
+        g_mean = self.grad.clone()
+        y = self.forward(torch.cat([u, u]), torch.cat([radius, radius]), seed, keep=True)
+        yv = y.detach().requires_grad_(True)
+        y1, y2 = yv[:nb], yv[nb:]
+        mse = ((0.5 * (y1 + y2) - target) ** 2).mean() - 0.25 * ((y1 - y2) ** 2).mean()
+        kmax = max(1, int(GRAIN_FMAX * min(h, w)))
+        with torch.no_grad():
+            pt = grain_power(target, u, n_target, kmax).float()
+            scale = (pt.abs() + mc_floor(target, n_target).float()[:, None]).mean(0) ** 2 + 1e-30
+        pd = radial_power((y1 - y2) * (1.0 / math.sqrt(2.0)), kmax)
+        spec = (((pd - pt) ** 2).mean(0) / scale).mean()
+        (mse + spec_weight * spec).backward()
+        self.backward_from(yv.grad)
+        self.grad.add_(g_mean)
+        self.adam_step(lr, ema_decay=ema_decay)
+        return mse.detach(), spec.detach()
 
     def use_ema(self):
         """Replace the weights by their moving average (done once training ends: the average of the
@@ -239,11 +301,15 @@ class SurrogateNet:
         self.w32.copy_(self.ema)
         self.wbf.copy_(self.w32.to(torch.bfloat16))
 
-    def infer(self, u, radius, seed: int, out=None):
-        """Whole-network forward through the single fg_sg_infer entry point; returns y [nb, h, w]."""
+    def infer(self, u, radius, seed: int, out=None, grain: bool = True):
+        """Whole-network forward through the single fg_sg_infer entry point; returns y [nb, h, w].
+        grain=False zeroes the noise channel's input weights: the network then predicts the expected
+        render instead of a grain realisation."""
         import torch
         nb, h, w = u.shape
         L = lib()
+        if not grain:
+            return self._mean_net().infer(u, radius, seed, out=out)
         need = L.fg_sg_infer_workspace_bytes(nb, h, w)
         if getattr(self, "_infer_ws", None) is None or self._infer_ws.numel() < need:
             self._infer_ws = torch.empty(need, dtype=torch.uint8, device=self.device)
@@ -253,6 +319,19 @@ class SurrogateNet:
         _raise(L.fg_sg_infer(ctypes.byref(net), u.data_ptr(), radius.data_ptr(), int(seed) & (2**64 - 1),
                              out.data_ptr(), nb, h, w, self._infer_ws.data_ptr(), self._infer_ws.numel(), _stream()))
         return out
+
+    def _mean_net(self) -> "SurrogateNet":
+        """A copy sharing nothing, with the noise channel's input weights zeroed (cached until the
+        weights change step)."""
+        import torch
+        key = (self.step, float(self.wbf.float().sum()))
+        if getattr(self, "_mean_key", None) != key:
+            m = SurrogateNet(self.n_res, self.radius_scale, device=str(self.device))
+            m.w32.copy_(self.w32)
+            m.view(m.w32, "w_in")[:, :, NOISE_CHANNEL] = 0.0
+            m.wbf.copy_(m.w32.to(torch.bfloat16))
+            self._mean, self._mean_key = m, key
+        return self._mean
 
 
 # ---------------------------------------------------------------------- training data
@@ -295,18 +374,33 @@ def training_tiles(n: int, size: int = 64, seed: int = 0, radius_range=(0.03, 0.
     return tiles, radius
 
 
+def training_set(n: int, size: int = 64, seed: int = 0, radius_range=(0.03, 0.2), lognormal_frac: float = 0.5,
+                 sd_frac: float = 0.4):
+    """training_tiles, with a lognormal radius distribution (standard deviation sd_frac x the mean) on a
+    share lognormal_frac of the tiles.  Returns (u [n, size, size], radius mean [n], radius standard
+    deviation [n] (0: constant), the network's radius input [n] (grain_radius))."""
+    u, radius = training_tiles(n, size, seed, radius_range)
+    rng = np.random.default_rng(seed + 7)
+    sd = np.where(rng.uniform(size=n) < lognormal_frac, sd_frac * radius, 0.0).astype(np.float32)
+    net_radius = np.array([grain_radius(float(r), float(v), v > 0) for r, v in zip(radius, sd)], np.float32)
+    return u, radius, sd, net_radius
+
+
 def render_tiles(u_tiles: np.ndarray, radius: np.ndarray, n_samples: int = 256, seed: int = 0,
-                 chunk: int = 1024, sigma_px: float = 0.8):
-    """Plain pixel-wise renders (the method of record) of each tile at its own radius, through batched
-    graphs of `chunk` tiles; returns a CUDA tensor [n, h, w] f32."""
+                 chunk: int = 1024, sigma_px: float = 0.8, radius_sd: Optional[np.ndarray] = None):
+    """Plain pixel-wise renders (the method of record) of each tile at its own radius (lognormal where
+    radius_sd is above 0, else constant), through batched graphs of `chunk` tiles; returns a CUDA tensor
+    [n, h, w] f32."""
     import torch
     n, h, w = u_tiles.shape
     out = torch.empty((n, h, w), dtype=torch.float32, device="cuda")
     for c0 in range(0, n, chunk):
         items = []
         for k in range(c0, min(n, c0 + chunk)):
-            p = ParamsBuilder(radius_mean=float(radius[k]), radius_dist=RadiusDist.Const, n_samples=n_samples,
-                              sigma_px=sigma_px, algo=Algo.Pixel, seed=(seed * 1_000_003 + k) & (2**64 - 1)).build()
+            sd = 0.0 if radius_sd is None else float(radius_sd[k])
+            p = ParamsBuilder(radius_mean=float(radius[k]), radius_dist=RadiusDist.Lognorm if sd > 0 else RadiusDist.Const,
+                              radius_stddev=sd, n_samples=n_samples, sigma_px=sigma_px, algo=Algo.Pixel,
+                              seed=(seed * 1_000_003 + k) & (2**64 - 1)).build()
             d = derive_common(p, (w, h))
             lam = lambda_plane(u_tiles[k], d.inv_e_pi_r2)
             items.append((torch.from_numpy(lam).cuda(), p, d, Algo.Pixel, lam))
@@ -321,10 +415,12 @@ def render_tiles(u_tiles: np.ndarray, radius: np.ndarray, n_samples: int = 256, 
 
 def train(net: SurrogateNet, u, radius, target, steps: int, batch: int = 256, lr: float = 1e-3, seed: int = 0,
           ema_decay: float = 0.999, log_every: int = 0, checkpoint: Optional[str] = None, checkpoint_every: int = 0,
-          log=print):
+          log=print, grain_n: Optional[int] = None, spec_weight: float = 0.01):
     """Adam training on (u, radius, target) CUDA tensors with a cosine learning-rate schedule from lr
-    down to lr/100 and a moving average of the weights (ema_decay).  Resumes from net.step (a loaded
-    checkpoint continues where it stopped).  Returns the list of (step, mean squared error) logged."""
+    down to lr/100 and a moving average of the weights (ema_decay).  grain_n: the targets' sample count,
+    for grain training (SurrogateNet.train_step_grain); None trains the plain mean-square objective.
+    Resumes from net.step (a loaded checkpoint continues where it stopped).  Returns the list of logged
+    (step, mean squared error) -- (step, paired MSE, spectral term) under grain training."""
     import torch
     n = u.shape[0]
     gen = torch.Generator(device="cpu")
@@ -336,11 +432,18 @@ def train(net: SurrogateNet, u, radius, target, steps: int, batch: int = 256, lr
         if s % 2 == 1:  # the integrators' statistics are isotropic: flip half the batches
             ub, tb = ub.flip(2).contiguous(), tb.flip(2).contiguous()
         step_lr = lr * (0.01 + 0.99 * 0.5 * (1.0 + math.cos(math.pi * s / max(1, steps))))
-        loss = net.train_step(ub, rb, tb, seed=seed * 7919 + s, lr=step_lr, ema_decay=ema_decay)
+        if grain_n:
+            mse, spec = net.train_step_grain(ub, rb, tb, seed=seed * 7919 + s, n_target=grain_n, lr=step_lr,
+                                             ema_decay=ema_decay, spec_weight=spec_weight)
+        else:
+            loss = net.train_step(ub, rb, tb, seed=seed * 7919 + s, lr=step_lr, ema_decay=ema_decay)
         if log_every and ((s + 1) % log_every == 0 or s + 1 == steps):
-            mse = float(loss.item()) / tb.numel()
-            history.append((s + 1, mse))
-            log(f"step {s + 1}: mse {mse:.3e}")
+            if grain_n:
+                history.append((s + 1, float(mse), float(spec)))
+                log(f"step {s + 1}: paired mse {float(mse):.3e}, spectral {float(spec):.3f}")
+            else:
+                history.append((s + 1, float(loss.item()) / tb.numel()))
+                log(f"step {s + 1}: mse {history[-1][1]:.3e}")
         if checkpoint and checkpoint_every and (s + 1) % checkpoint_every == 0:
             net.save(checkpoint)
     return history
@@ -362,6 +465,98 @@ def raps(img):
     sums = torch.bincount(r, weights=p.flatten(), minlength=nb + 1)
     cnts = torch.bincount(r, minlength=nb + 1)
     return sums[1:nb + 1] / cnts[1:nb + 1].clamp(min=1)
+
+
+def grain_radius(radius_mean: float, radius_stddev: float = 0.0, lognormal: bool = False) -> float:
+    """The radius input for a radius distribution: the constant radius whose grains give the same grain
+    power.  The low-frequency grain power of sparse grains is proportional to E[r^4] / E[r^2]; for a
+    lognormal radius of mean m and standard deviation s (shape s2 = ln(1 + s^2 / m^2)) that is
+    (m (1 + s^2 / m^2)^2.5)^2.  The network is trained on constant radii."""
+    if not lognormal or radius_stddev <= 0.0:
+        return float(radius_mean)
+    return float(radius_mean * (1.0 + (radius_stddev / radius_mean) ** 2) ** 2.5)
+
+
+def expected_render(u, sigma_px: float = 0.8):
+    """The expectation of a plain zoom-1 render given u [nb, h, w]: each sample lands d pixels from its
+    pixel with probability Phi((d + 1/2) / sigma) - Phi((d - 1/2) / sigma) per axis (Gaussian offsets of
+    the filter's sigma), where the grains cover the fraction u; edge pixels extend outwards, as the
+    renderer clamps its lambda lookups to the plane."""
+    import torch
+    import torch.nn.functional as F
+    r = int(math.ceil(4.0 * sigma_px))
+    d = torch.arange(-r, r + 1, dtype=torch.float64)
+    cdf = lambda z: 0.5 * (1.0 + torch.erf(z / math.sqrt(2.0)))
+    k = cdf((d + 0.5) / sigma_px) - cdf((d - 0.5) / sigma_px)
+    k = (k / k.sum()).to(device=u.device, dtype=u.dtype)
+    x = F.pad(u[:, None], (r, r, r, r), mode="replicate")
+    x = F.conv2d(F.conv2d(x, k.view(1, 1, 1, -1)), k.view(1, 1, -1, 1))
+    return x[:, 0]
+
+
+_BINS: Dict[Tuple[int, int, int, str], object] = {}
+
+
+def radial_power(x, kmax: int):
+    """Radial power spectrum per image of x [nb, h, w]: the mean |FFT|^2 of (x - its mean) over the annuli
+    of integer radius 1 .. kmax (radius k = k / size cycles per pixel on a square image).  Returns
+    [nb, kmax]; differentiable (a binning matrix for tiles up to 256^2, bin sums beyond)."""
+    import torch
+    nb, h, w = x.shape
+    a = x - x.mean(dim=(1, 2), keepdim=True)
+    f = torch.fft.fft2(a)
+    p = (f.real ** 2 + f.imag ** 2).reshape(nb, h * w)
+    key = (h, w, kmax, str(x.device))
+    m = _BINS.get(key)
+    if m is None:
+        fy = torch.fft.fftfreq(h, device=x.device, dtype=torch.float64) * h
+        fx = torch.fft.fftfreq(w, device=x.device, dtype=torch.float64) * w
+        r = torch.round(torch.sqrt(fy[:, None] ** 2 + fx[None, :] ** 2)).long().flatten()
+        if h * w <= 256 * 256:
+            sel = (r >= 1) & (r <= kmax)
+            m = torch.zeros(h * w, kmax, dtype=torch.float64, device=x.device)
+            m[torch.nonzero(sel).flatten(), r[sel] - 1] = 1.0
+            m = m / m.sum(0).clamp(min=1.0)
+        else:
+            m = r
+        _BINS[key] = m
+    if m.dim() == 2:
+        return p @ m.to(p.dtype)
+    out = torch.zeros(nb, kmax, dtype=torch.float64, device=x.device)
+    sel = (m >= 1) & (m <= kmax)
+    cnt = torch.bincount(m[sel] - 1, minlength=kmax).clamp(min=1)
+    for b in range(nb):
+        out[b] = torch.bincount(m[sel] - 1, weights=p[b][sel].double(), minlength=kmax) / cnt
+    return out
+
+
+def mc_floor(img, n_samples: int):
+    """Per image: the radial power of a plain render's Monte Carlo error, white with variance f (1 - f) / N
+    per pixel (f the render itself), in radial_power's units (h w times the variance)."""
+    h, w = img.shape[-2:]
+    return h * w * (img * (1.0 - img)).double().mean(dim=(1, 2)) / float(n_samples)
+
+
+def grain_power(img, u, n_samples: Optional[int], kmax: int):
+    """Radial power of the grain of a render img [nb, h, w] of intensities u: the spectrum of its residual
+    against the expectation (expected_render), less the Monte Carlo floor of a plain render at n_samples
+    (None for a render without Monte Carlo error: a prediction)."""
+    p = radial_power(img - expected_render(u), kmax)
+    if n_samples:
+        p = p - mc_floor(img, n_samples).to(p.dtype)[:, None]
+    return p
+
+
+def grain_band_error(pred, ref, u, n_pred: Optional[int], n_ref: Optional[int], fmax: float = 0.25) -> float:
+    """||G_pred - G_ref||_2 / ||G_ref||_2 over the radial bins up to fmax cycles/px, G the grain power
+    (grain_power) averaged over the images: how far pred's grain is from ref's in spectrum.  A prediction
+    without grain (u itself, the expectation) scores about 1."""
+    if pred.dim() == 2:
+        pred, ref, u = pred[None], ref[None], u[None]
+    kmax = max(1, int(fmax * min(pred.shape[-2:])))
+    gp = grain_power(pred, u, n_pred, kmax).double().mean(0)
+    gr = grain_power(ref, u, n_ref, kmax).double().mean(0)
+    return float(torch_norm(gp - gr) / torch_norm(gr))
 
 
 def raps_error(pred, ref) -> float:
@@ -392,7 +587,8 @@ DEFAULT_WEIGHTS = _os.path.join(_os.path.dirname(_os.path.abspath(__file__)), "w
 
 def load_default(device: str = "cuda") -> SurrogateNet:
     """The shipped network: trained by ``python -m film_grain_gb300.surrogate train`` on 20,000 64x64
-    luma tiles rendered by the plain pixel-wise method at N=256 (radius U[0.03, 0.2], sigma 0.8)."""
+    luma tiles rendered by the plain pixel-wise method at N=256 (radius mean U[0.03, 0.2], constant on
+    half the tiles and lognormal with standard deviation 0.4 x the mean on the others; sigma 0.8)."""
     if not _os.path.exists(DEFAULT_WEIGHTS):
         raise FileNotFoundError(f"surrogate weights missing: {DEFAULT_WEIGHTS}")
     return SurrogateNet.load(DEFAULT_WEIGHTS, device=device)
@@ -401,15 +597,16 @@ def load_default(device: str = "cuda") -> SurrogateNet:
 def train_from_scratch(tiles: int = 20000, tile_size: int = 64, n_samples: int = 256, steps: int = 8000,
                        batch: int = 256, lr: float = 1e-3, seed: int = 0, n_res: int = 8,
                        checkpoint: Optional[str] = None, checkpoint_every: int = 500, resume: bool = False,
-                       log=print) -> Tuple[SurrogateNet, dict]:
+                       log=print, grain: bool = True, spec_weight: float = 0.01) -> Tuple[SurrogateNet, dict]:
     """Render the training tiles with the plain method and train a network on them (resuming from
-    `checkpoint` when resume=True and it exists).  Returns (net, info)."""
+    `checkpoint` when resume=True and it exists): grain training (train_step_grain) unless grain=False,
+    which trains the expectation alone.  Returns (net, info)."""
     import time
     import torch
     t0 = time.time()
-    u, r = training_tiles(tiles, tile_size, seed=seed + 1)
+    u, r, sd, r_net = training_set(tiles, tile_size, seed=seed + 1)
     t1 = time.time()
-    target = render_tiles(u, r, n_samples=n_samples, seed=seed + 1)
+    target = render_tiles(u, r, n_samples=n_samples, seed=seed + 1, radius_sd=sd)
     torch.cuda.synchronize()
     t2 = time.time()
     log(f"tiles: {tiles} x {tile_size}^2 generated in {t1 - t0:.1f} s, rendered at N={n_samples} in {t2 - t1:.1f} s")
@@ -418,14 +615,17 @@ def train_from_scratch(tiles: int = 20000, tile_size: int = 64, n_samples: int =
         log(f"resumed from {checkpoint} at step {net.step}")
     else:
         net = SurrogateNet(n_res=n_res, seed=seed)
-    ut, rt = torch.from_numpy(u).cuda(), torch.from_numpy(r).cuda()
+    ut, rt = torch.from_numpy(u).cuda(), torch.from_numpy(r_net).cuda()
     hist = train(net, ut, rt, target, steps=steps, batch=batch, lr=lr, seed=seed, log_every=max(1, steps // 10),
-                 checkpoint=checkpoint, checkpoint_every=checkpoint_every, log=log)
+                 checkpoint=checkpoint, checkpoint_every=checkpoint_every, log=log,
+                 grain_n=n_samples if grain else None, spec_weight=spec_weight)
     net.use_ema()
     torch.cuda.synchronize()
     t3 = time.time()
     info = dict(tiles=tiles, tile_size=tile_size, n_samples=n_samples, steps=steps, batch=batch, lr=lr, seed=seed,
-                render_s=t2 - t1, train_s=t3 - t2, final_mse=hist[-1][1] if hist else float("nan"))
+                render_s=t2 - t1, train_s=t3 - t2, final_mse=hist[-1][1] if hist else float("nan"),
+                objective="grain (paired MSE + spectral)" if grain else "MSE", spec_weight=spec_weight if grain else 0.0,
+                final_spectral=hist[-1][2] if hist and grain else float("nan"))
     log(f"trained {steps} steps (batch {batch}) in {t3 - t2:.1f} s")
     return net, info
 
@@ -447,11 +647,14 @@ def main(argv=None):
     t.add_argument("--checkpoint", default=None, help="checkpoint with Adam moments, written every --checkpoint-every")
     t.add_argument("--checkpoint-every", type=int, default=500)
     t.add_argument("--resume", action="store_true", help="continue from --checkpoint")
+    t.add_argument("--mean-only", action="store_true", help="train the expectation alone (no grain)")
+    t.add_argument("--spec-weight", type=float, default=0.01, help="weight of the spectral term of grain training")
     a = ap.parse_args(argv)
     from .build import build
     build()
     net, info = train_from_scratch(a.tiles, a.tile_size, a.n_samples, a.steps, a.batch, a.lr, a.seed, a.n_res,
-                                   a.checkpoint, a.checkpoint_every, a.resume)
+                                   a.checkpoint, a.checkpoint_every, a.resume, grain=not a.mean_only,
+                                   spec_weight=a.spec_weight)
     _os.makedirs(_os.path.dirname(_os.path.abspath(a.out)), exist_ok=True)
     net.save(a.out, optimizer=False, **info)
     print(f"wrote {a.out}")

@@ -80,3 +80,78 @@ def test_raps_of_known_signals():
     # white noise: flat spectrum with mean power n^2 * variance
     assert abs(white[8:].mean() / (256 * 256) - 1.0) < 0.05
     assert np.allclose(sr.raps(np.full((16, 16), 3.0)), 0.0)
+
+
+def _sg():
+    import pytest
+    torch = pytest.importorskip("torch")
+    from film_grain_gb300 import surrogate
+    return torch, surrogate
+
+
+def test_radial_power_of_white_noise_and_gradient():
+    """White noise of variance v has radial power h*w*v in every bin; the binning-matrix path and the
+    bin-sum path (large planes) agree; the power is differentiable through the FFT."""
+    torch, sg = _sg()
+    g = torch.Generator().manual_seed(1)
+    x = torch.randn(8, 64, 64, generator=g, dtype=torch.float64) * 0.5
+    p = sg.radial_power(x, 40)
+    assert abs(float(p[:, 4:].mean()) / (64 * 64 * 0.25) - 1.0) < 0.05
+    big = torch.randn(1, 512, 512, generator=g, dtype=torch.float64)
+    pb = sg.radial_power(big, 200)  # bin-sum path
+    assert abs(float(pb[0, 8:].mean()) / (512 * 512) - 1.0) < 0.05
+    # one small image through both paths: the bin-sum path equals the matrix path bin for bin
+    m = sg.radial_power(x[:1], 30)
+    sg._BINS[(64, 64, 30, str(x.device))] = None
+    key = (64, 64, 30, str(x.device))
+    fy = torch.fft.fftfreq(64, dtype=torch.float64) * 64
+    r = torch.round(torch.sqrt(fy[:, None] ** 2 + fy[None, :] ** 2)).long().flatten()
+    sg._BINS[key] = r
+    assert torch.allclose(sg.radial_power(x[:1], 30), m, rtol=1e-10)
+    del sg._BINS[key]
+    y = x.clone().requires_grad_(True)
+    sg.radial_power(y, 10).sum().backward()
+    assert float(y.grad.abs().sum()) > 0
+
+
+def test_expected_render_weights():
+    """The expectation filter is the box-integrated Gaussian: it keeps constants, spreads a single bright
+    pixel by Phi((d + 1/2)/sigma) - Phi((d - 1/2)/sigma) per axis, and replicates the edges."""
+    import math
+    torch, sg = _sg()
+    u = torch.full((1, 16, 16), 0.3, dtype=torch.float64)
+    assert torch.allclose(sg.expected_render(u), u)
+    d = torch.zeros((1, 17, 17), dtype=torch.float64)
+    d[0, 8, 8] = 1.0
+    e = sg.expected_render(d)
+    phi = lambda z: 0.5 * (1.0 + math.erf(z / math.sqrt(2.0)))
+    w1 = (phi(1.5 / 0.8) - phi(0.5 / 0.8))
+    w0 = (phi(0.5 / 0.8) - phi(-0.5 / 0.8))
+    tot = sum(phi((k + 0.5) / 0.8) - phi((k - 0.5) / 0.8) for k in range(-4, 5))
+    assert abs(float(e[0, 8, 9]) - w0 * w1 / tot ** 2) < 1e-12
+    assert abs(float(e.sum()) - 1.0) < 1e-12
+
+
+def test_grain_radius_and_band_error():
+    """The lognormal radius maps to the constant radius of equal E[r^4]/E[r^2] (checked by sampling);
+    grain_band_error is 0 for identical grain, about 1 for a prediction without grain, and the Monte
+    Carlo floor of a plain render is removed before the comparison."""
+    import numpy as np
+    torch, sg = _sg()
+    m, s = 0.025, 0.01
+    s2 = np.log(1.0 + (s / m) ** 2)
+    r = np.random.default_rng(2).lognormal(np.log(m) - s2 / 2, np.sqrt(s2), 2_000_000)
+    assert abs(sg.grain_radius(m, s, lognormal=True) / np.sqrt(np.mean(r ** 4) / np.mean(r ** 2)) - 1.0) < 0.01
+    assert sg.grain_radius(0.1) == 0.1
+    g = torch.Generator().manual_seed(3)
+    u = torch.full((4, 64, 64), 0.5, dtype=torch.float64)
+    grain = sg.expected_render(torch.randn(4, 64, 64, generator=g, dtype=torch.float64)) * 0.2
+    ref = u + grain
+    assert sg.grain_band_error(ref, ref, u, None, None) == 0.0
+    assert abs(sg.grain_band_error(u, ref, u, None, None) - 1.0) < 1e-9
+    # a plain render at N = 64 carries white Monte Carlo noise of variance f (1 - f) / N on top: with the
+    # floor removed its grain matches; without, the noise counts as grain
+    noisy = ref + torch.randn(4, 64, 64, generator=g, dtype=torch.float64) * np.sqrt(0.25 / 64)
+    with_floor = sg.grain_band_error(noisy, ref, u, 64, None, fmax=0.5)
+    without = sg.grain_band_error(noisy, ref, u, None, None, fmax=0.5)
+    assert with_floor < 0.1 and without > 2.0 * with_floor, (with_floor, without)
