@@ -62,6 +62,10 @@ WORKLOADS = {
                                         "(the per-sample kernel)",
                                    w=2048, h=2048, mode="luma", algo="pixel", radius=0.025, dist="const", sd=0.0,
                                    zoom=1.0, n=64, seed=42, image_seed=5, source="blobs"),
+    "pixel_luma_1024_flat": dict(desc="profiling case: pixel-wise luma 1024x1024 flat plane u = 0.13 (the 4096^2 "
+                                      "frame's background), lognormal r 0.025/0.01, N 256, zoom 1",
+                                 w=1024, h=1024, mode="luma", algo="pixel", radius=0.025, dist="lognorm", sd=0.01,
+                                 zoom=1.0, n=256, seed=42, image_seed=0, source="flat", level=0.13),
     "pixel_rgb_4096": dict(desc="plain pixel-wise RGB 4096x4096x3 blobs, lognormal r 0.025/0.01, N 256, zoom 1",
                            w=4096, h=4096, mode="rgb", algo="pixel", radius=0.025, dist="lognorm", sd=0.01, zoom=1.0,
                            n=256, seed=42, image_seed=1),
@@ -197,14 +201,15 @@ def cpu_pixel_baseline(oracle, planes, wl, threads, rows=None):
 
 
 # DRAM bytes per launch from ncu captures of the dominant kernels on their profiling cases (the
-# --profile-once runs), per unit of work: sg_conv_fwd<32,32,residual> on the 1024^2 x 3 surrogate input,
-# 358.6 MB read+write for 3 x 1024^2 px; grainwise_persistent_kernel on a 512^2 -> 1024^2 plane of the
-# grain-wise blob frame, 18.25 MB per 1024^2 output pixels (the lambda plane plus the sample-mask lines
-# that miss L2); the pixel-wise lean and deferred block passes on plane 0 of the 4096^2 x 3 frame,
-# 458.7 MB per 4096^2 output pixels.
-SG_CONV_DRAM_BYTES_PER_PX = 358.6e6 / (3 * 1024 * 1024)
+# --profile-once runs), per unit of work: sg_conv32_tc_kernel (the residual conv) on the 1024^2 x 3
+# surrogate input, 373.9 MB read+write for 3 x 1024^2 px; grainwise_persistent_kernel on a 512^2 ->
+# 1024^2 plane of the grain-wise blob frame, 18.25 MB per 1024^2 output pixels (the lambda plane plus the
+# sample-mask lines that miss L2); cell_mask_kernel + pixelwise_sparse_kernel on the 1024^2 flat plane
+# of the large frame's parameters, 170.3 + 250.0 MB per 1024^2 output pixels (the emptiness bitmask
+# written, then read with the cell table).
+SG_CONV_DRAM_BYTES_PER_PX = 373.9e6 / (3 * 1024 * 1024)
 GRAINWISE_DRAM_BYTES_PER_OUT_PX = 18.25e6 / (1024 * 1024)
-PIXELWISE_DRAM_BYTES_PER_OUT_PX = (399.3e6 + 59.4e6) / (4096 * 4096)
+PIXELWISE_DRAM_BYTES_PER_OUT_PX = (170.3e6 + 250.0e6) / (1024 * 1024)
 
 # Algorithmic lane-ops of the pixel-wise path (an exact method that hashes every cell once): per cell
 # its hash and first uniform (~65: the row stage of mix3, one SplitMix64, ~24; the four PCG32 seed words
@@ -370,8 +375,8 @@ def surrogate_compare(fg, sg, net, steps, warmup, plain_steps, clocks=None, seed
     # the same network with its noise input off predicts the expectation instead of a grain realisation
     y_mean = net.infer(u_dev, radius, seed=seed, grain=False)
     q_mean = sg.evaluate(y_mean, ref1024)
-    # grain-band spectrum error (radial bins up to 0.25 cycles/px of each render's residual against the
-    # expectation, Monte Carlo floors of plain renders removed) against the N=1024 render
+    # grain-band spectrum error (radial bins from 1/64 to 1/4 cycles/px of each render's residual against
+    # the expectation, Monte Carlo floors of plain renders removed) against the N=1024 render
     grain_band = {"surrogate": sg.grain_band_error(y, ref1024, u_dev, None, 1024),
                   "surrogate_no_noise": sg.grain_band_error(y_mean, ref1024, u_dev, None, 1024),
                   "identity": sg.grain_band_error(u_dev, ref1024, u_dev, None, 1024),
@@ -430,15 +435,19 @@ def surrogate_line(steps, warmup, world, retrain=False, cpu=True):
                         "surrogate_no_noise_vs_n1024": r["q_mean"],
                         "grain_band_error_vs_n1024": r["grain_band"],
                         "targets": {"mae": 0.01, "raps": 0.02}},
-            "roofline": {"bound": "tensor", "achieved": ach, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-                         "frac": ach / peaks["bf16_tflops"],
+            # the 32 -> 32 residual conv: 18.4 kFLOP and 128 B (64 B in, 64 B out) per pixel, 144 FLOP/B,
+            # below the GB300's ridge (bf16 peak / HBM bandwidth): HBM-bound
+            "roofline": {"bound": "hbm", "achieved": r["conv_bytes"] / (r["conv_ms"] / 1e3) / 1e9,
+                         "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": r["conv_bytes"] / (r["conv_ms"] / 1e3) / (peaks["hbm_gbs"] * 1e9),
                          "traffic": SG_CONV_DRAM_BYTES_PER_PX * 3 * r["size"] ** 2,
-                         "traffic_basis": "ncu dram bytes of sg_conv_fwd<32,32,residual> on the 1024^2 x 3 "
-                                          "surrogate input, scaled by pixels",
-                         "kernel": "sg_conv_fwd<32,32,residual>", "launch_ms": r["conv_ms"],
-                         "flop_per_launch": r["conv_flop"], "algorithmic_bytes_per_launch": r["conv_bytes"],
-                         "hbm_frac": r["conv_bytes"] / (r["conv_ms"] / 1e3) / (peaks["hbm_gbs"] * 1e9),
-                         "peak_basis": f"bf16 burst, {basis}"},
+                         "traffic_basis": "ncu dram bytes of sg_conv32_tc_kernel on the 1024^2 x 3 surrogate "
+                                          "input, scaled by pixels",
+                         "kernel": "sg_conv32_tc_kernel (tcgen05, one residual layer of the 4096^2 x 3 frame)",
+                         "launch_ms": r["conv_ms"], "flop_per_launch": r["conv_flop"],
+                         "algorithmic_bytes_per_launch": r["conv_bytes"], "tensor_tflops": ach,
+                         "tensor_frac": ach / peaks["bf16_tflops"], "tensor_peak": peaks["bf16_tflops"],
+                         "peak_basis": f"HBM copy and bf16 burst, {basis}"},
             "e2e": {"value": r["e2e_ms"], "unit": "ms/frame", "h2d_bytes_per_step": r["h2d"] + 12,
                     "d2h_bytes_per_step": r["d2h"], "path": "pinned f32 u planes -> fg_sg_infer -> pinned f32 planes"},
             "gpu_launches": steps * r["launches_per_frame"], "clocks": r["clocks"]}
@@ -555,6 +564,22 @@ def batch_line(steps, warmup, world):
     return line
 
 
+def replica_max(dist, value, device):
+    """The largest of the ranks' values: a barrier, then an all-reduce MAX of one float (the whole job's
+    time is its slowest replica's)."""
+    import torch
+    dist.barrier()
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(samples_per_frame, steps, world, elapsed):
+    """Whole-job throughput of `world` replicas that each render `steps` frames, the job's time being the
+    slowest replica's `elapsed` seconds."""
+    return samples_per_frame * steps * world / elapsed
+
+
 def plain_line(wl_name, steps, warmup, rank=0, world=1, dist=None, cpu=True, e2e_steps=None):
     """One plain workload (WORKLOADS[wl_name]) through the per-plane render calls: returns the line
     (rank 0) or None (other ranks)."""
@@ -613,14 +638,11 @@ def plain_line(wl_name, steps, warmup, rank=0, world=1, dist=None, cpu=True, e2e
                  for c in range(len(planes))]  # mean duration of plane c's render call
     elapsed = t_start.elapsed_time(t_end) / 1e3
     if dist:
-        dist.barrier()
-        tt = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        elapsed = float(tt.item())
+        elapsed = replica_max(dist, elapsed, "cuda")
     clk = clocks.stop() if clocks else None
 
     samples_per_frame = ow * oh * len(planes) * wl["n"]
-    value = samples_per_frame * steps * world / elapsed
+    value = replica_value(samples_per_frame, steps, world, elapsed)
     ms_per_step = elapsed / steps * 1e3
 
     # ---- end to end through the public entry point, pinned host buffers
@@ -698,9 +720,9 @@ def plain_line(wl_name, steps, warmup, rank=0, world=1, dist=None, cpu=True, e2e
         line["roofline"] = {"bound": "sm_issue", "achieved": ach / 1e12, "peak": peak / 1e12, "unit": "Tlane-op/s",
                             "frac": ach / peak,
                             "traffic": PIXELWISE_DRAM_BYTES_PER_OUT_PX * ow * oh,
-                            "traffic_basis": "ncu dram bytes of the plane's kernels (cell table, emptiness bitmask, "
-                                             "sparse and deferred block passes, epilogue) on plane 0 of the "
-                                             "4096^2 x 3 frame, scaled by output pixels",
+                            "traffic_basis": "ncu dram bytes of cell_mask_kernel + pixelwise_sparse_kernel on the "
+                                             "1024^2 flat plane of the large frame's parameters, scaled by "
+                                             "output pixels",
                             "kernel": "cell_mask_kernel + pixelwise_sparse_kernel + pixelwise_deferred_kernel "
                                       "(launch_ms: the whole render call of a plane)", "launch_ms": launch_ms,
                             "lane_ops_per_launch": [o["total"] for o in ops], "model_terms": ops[0],

@@ -260,10 +260,11 @@ class SurrogateNet:
                          ema_decay: float = 0.999, spec_weight: float = 0.01):
         """One Adam step of grain training on a batch of tiles (see the module docstring): the network runs
         on every tile twice, with two noise fields, and the loss is the paired mean-square term plus
-        spec_weight x the spectral term: per radial bin, the mean square difference between the pairs'
-        noise-part power and the targets' grain power (target renders at n_target samples), relative to
-        the bin's mean grain power plus the Monte Carlo floor -- so power the network adds where the
-        targets have no grain (high frequencies) costs as much as power missing where they have it.  A
+        spec_weight x the spectral term: per tile and radial bin, the square difference between the pairs'
+        noise-part power and the target's grain power (target renders at n_target samples), relative to
+        the tile's mean square grain power plus Monte Carlo floor (plus a tenth of the batch mean) -- so
+        power the network adds where the target has no grain (high frequencies) costs as much as power
+        missing where it has it, and a small-radius tile weighs about as much as a large-radius one.  A
         third pass, with the noise channel's input weights zeroed, adds the plain mean-square error of
         that network (the expectation predictor; the zeroed weights get no gradient from it).
         Returns (paired MSE, spectral term) tensors."""
@@ -285,9 +286,14 @@ class SurrogateNet:
         kmax = max(1, int(GRAIN_FMAX * min(h, w)))
         with torch.no_grad():
             pt = grain_power(target, u, n_target, kmax).float()
-            scale = (pt.abs() + mc_floor(target, n_target).float()[:, None]).mean(0) ** 2 + 1e-30
+            floor = mc_floor(target, n_target).float()[:, None]
+            # per tile, relative to its own grain power plus floor, so that small radii (whose grain
+            # carries a hundredth of the power of the largest) count; a tenth of the batch's mean scale
+            # is added, so that a flat black or white tile (no grain, no floor) cannot dominate
+            tile = ((pt.abs() + floor) ** 2).mean(1, keepdim=True)
+            scale = tile + 0.1 * tile.mean() + 1e-30
         pd = radial_power((y1 - y2) * (1.0 / math.sqrt(2.0)), kmax)
-        spec = (((pd - pt) ** 2).mean(0) / scale).mean()
+        spec = (((pd - pt) ** 2) / scale).mean()
         (mse + spec_weight * spec).backward()
         self.backward_from(yv.grad)
         self.grad.add_(g_mean)
@@ -547,15 +553,20 @@ def grain_power(img, u, n_samples: Optional[int], kmax: int):
     return p
 
 
-def grain_band_error(pred, ref, u, n_pred: Optional[int], n_ref: Optional[int], fmax: float = 0.25) -> float:
-    """||G_pred - G_ref||_2 / ||G_ref||_2 over the radial bins up to fmax cycles/px, G the grain power
-    (grain_power) averaged over the images: how far pred's grain is from ref's in spectrum.  A prediction
-    without grain (u itself, the expectation) scores about 1."""
+def grain_band_error(pred, ref, u, n_pred: Optional[int], n_ref: Optional[int], fmax: float = 0.25,
+                     fmin: float = 1.0 / 64.0) -> float:
+    """||G_pred - G_ref||_2 / ||G_ref||_2 over the radial bins from fmin to fmax cycles/px, G the grain
+    power (grain_power) averaged over the images: how far pred's grain is from ref's in spectrum.  A
+    prediction without grain (u itself, the expectation) scores about 1.  The band starts at wavelengths
+    of 64 px: below that, on large frames, the image content's own spectrum is so strong that any
+    departure from the expectation's exact level outweighs the grain."""
     if pred.dim() == 2:
         pred, ref, u = pred[None], ref[None], u[None]
-    kmax = max(1, int(fmax * min(pred.shape[-2:])))
-    gp = grain_power(pred, u, n_pred, kmax).double().mean(0)
-    gr = grain_power(ref, u, n_ref, kmax).double().mean(0)
+    size = min(pred.shape[-2:])
+    kmax = max(1, int(fmax * size))
+    k0 = min(kmax, max(1, int(math.ceil(fmin * size))))
+    gp = grain_power(pred, u, n_pred, kmax).double().mean(0)[k0 - 1:]
+    gr = grain_power(ref, u, n_ref, kmax).double().mean(0)[k0 - 1:]
     return float(torch_norm(gp - gr) / torch_norm(gr))
 
 
@@ -594,7 +605,7 @@ def load_default(device: str = "cuda") -> SurrogateNet:
     return SurrogateNet.load(DEFAULT_WEIGHTS, device=device)
 
 
-def train_from_scratch(tiles: int = 20000, tile_size: int = 64, n_samples: int = 256, steps: int = 8000,
+def train_from_scratch(tiles: int = 20000, tile_size: int = 64, n_samples: int = 256, steps: int = 4000,
                        batch: int = 256, lr: float = 1e-3, seed: int = 0, n_res: int = 8,
                        checkpoint: Optional[str] = None, checkpoint_every: int = 500, resume: bool = False,
                        log=print, grain: bool = True, spec_weight: float = 0.01) -> Tuple[SurrogateNet, dict]:
@@ -638,7 +649,7 @@ def main(argv=None):
     t.add_argument("--tiles", type=int, default=20000)
     t.add_argument("--tile-size", type=int, default=64)
     t.add_argument("--n-samples", type=int, default=256)
-    t.add_argument("--steps", type=int, default=8000)
+    t.add_argument("--steps", type=int, default=4000)
     t.add_argument("--batch", type=int, default=256)
     t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--seed", type=int, default=0)

@@ -152,34 +152,42 @@ def test_checkpoint_resume(sg, cuda, tmp_path):
 
 
 def test_training_gains_over_no_network(sg, cuda):
-    """A short training run on plain N=256 tile renders.  On held-out tiles, scored against the expected
-    render (the mean of 16 independently seeded N=1024 plain renders: a single render carries MC noise
-    and a grain realisation no predictor can know), the trained network's MAE beats (a) the method
-    without a network (the intensity u itself) and (b) the untrained network by 2x, and (c) the plain
-    render at N=16."""
+    """A short grain-training run on plain N=256 renders of tiles (constant and lognormal radii), scored
+    on held-out tiles.
+    (a) With its noise weights zeroed the network predicts the expected render (the mean of 16
+        independently seeded N=1024 renders: a single render carries a grain realisation and MC noise no
+        predictor can know) with less than half the MAE of the method without a network (the intensity u
+        itself) and of the untrained network, and beats the plain render at N=16.
+    (b) With its noise input it renders grain: the spectrum of its residual against the expectation over
+        1/64 .. 1/4 cycles/px is within half the error of u's (u has no grain) from the grain of a plain
+        N=1024 render."""
     torch = cuda
-    u_tr, r_tr = sg.training_tiles(4096, seed=1)
-    t_tr = sg.render_tiles(u_tr, r_tr, n_samples=256, seed=1)
-    u_te, r_te = sg.training_tiles(128, seed=99)
-    refs = [sg.render_tiles(u_te, r_te, n_samples=1024, seed=99 + k) for k in range(16)]
+    u_tr, r_tr, sd_tr, rn_tr = sg.training_set(4096, seed=1)
+    t_tr = sg.render_tiles(u_tr, r_tr, n_samples=256, seed=1, radius_sd=sd_tr)
+    u_te, r_te, sd_te, rn_te = sg.training_set(128, seed=99)
+    refs = [sg.render_tiles(u_te, r_te, n_samples=1024, seed=99 + k, radius_sd=sd_te) for k in range(16)]
     ref = sum(refs) / 16
-    low = sg.render_tiles(u_te, r_te, n_samples=16, seed=123)
-    ut, rt = torch.from_numpy(u_tr).cuda(), torch.from_numpy(r_tr).cuda()
-    ue, re = torch.from_numpy(u_te).cuda(), torch.from_numpy(r_te).cuda()
+    low = sg.render_tiles(u_te, r_te, n_samples=16, seed=123, radius_sd=sd_te)
+    ut, rt = torch.from_numpy(u_tr).cuda(), torch.from_numpy(rn_tr).cuda()
+    ue, re = torch.from_numpy(u_te).cuda(), torch.from_numpy(rn_te).cuda()
     net = sg.SurrogateNet(n_res=8, seed=0)
-    mae_untrained = float((net.infer(ue, re, seed=5) - ref).abs().mean())
-    hist = sg.train(net, ut, rt, t_tr, steps=2000, batch=64, lr=1e-3, seed=0, log_every=500, log=lambda s: None)
+    mae_untrained = float((net.infer(ue, re, seed=5, grain=False) - ref).abs().mean())
+    hist = sg.train(net, ut, rt, t_tr, steps=2000, batch=64, lr=1e-3, seed=0, log_every=500, log=lambda s: None,
+                    grain_n=256)
     net.use_ema()
-    mae_net = float((net.infer(ue, re, seed=5) - ref).abs().mean())
+    mae_net = float((net.infer(ue, re, seed=5, grain=False) - ref).abs().mean())
     mae_id = float((ue - ref).abs().mean())
     mae_low = float((low - ref).abs().mean())
     floor = float((refs[0] - refs[1]).abs().mean()) / np.sqrt(2)  # one N=1024 render's own deviation
+    gb_net = sg.grain_band_error(net.infer(ue, re, seed=5), refs[0], ue, None, 1024)
+    gb_id = sg.grain_band_error(ue, refs[0], ue, None, 1024)
     print(f"MAE vs mean of 16 N=1024 renders: trained {mae_net:.4f}, identity {mae_id:.4f}, "
           f"untrained {mae_untrained:.4f}, plain N=16 {mae_low:.4f}, single N=1024 render {floor:.4f}; "
-          f"train mse {hist}")
+          f"grain-band error vs an N=1024 render: trained {gb_net:.3f}, identity {gb_id:.3f}; train {hist}")
     assert mae_net < 0.5 * mae_id
     assert mae_net < 0.5 * mae_untrained
     assert mae_net < mae_low
+    assert gb_net < 0.5 * gb_id
 
 
 def test_evaluator_matches_oracle(sg, cuda):
