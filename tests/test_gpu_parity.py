@@ -145,6 +145,21 @@ def test_pixelwise_lognormal_small_radius(cuda, fgl, orc):
     _check("pixel", fgl, orc, _blobs(40, 32), radius=0.025, dist="lognorm", sd=0.01, n=256, seed=31)
 
 
+@pytest.mark.parametrize("n,zoom,dist,radius", [(256, 1.0, "lognorm", 0.04), (64, 1.0, "const", 0.08),
+                                                (16, 1.0, "lognorm", 0.15), (256, 2.0, "lognorm", 0.04),
+                                                (100, 0.5, "const", 0.1)])
+def test_pixelwise_sparse_pass_forms(cuda, fgl, orc, n, zoom, dist, radius):
+    """The sparse block pass (6 launches) in its forms: one offset per thread (N = 256) or several
+    threads per offset sharing its rows (N 64, 16); rectangles within the 4 x 4 range table (zoom 1) or
+    beyond it (zoom 2: cell ranges computed per sample); zoom 0.5; on a plane large enough for the
+    4 x 4-pixel blocks, mixing dense and sparse regions."""
+    plane = _blobs(160, 128, seed=5)
+    kw = dict(radius=radius, dist=dist, sd=0.4 * radius if dist == "lognorm" else 0.0, zoom=zoom, n=n, seed=41)
+    p, d, *_ = _setup(fgl, orc, plane, **kw)
+    assert fgl.pixelwise_kernel_count(p, d) == 6
+    _check("pixel", fgl, orc, plane, **kw)
+
+
 def test_pixelwise_empty_and_tiny(cuda, fgl, orc):
     _check("pixel", fgl, orc, np.zeros((16, 16), np.float32), radius=0.1, n=8)
     _check("pixel", fgl, orc, np.full((1, 1), 0.5, np.float32), radius=0.1, n=8)
