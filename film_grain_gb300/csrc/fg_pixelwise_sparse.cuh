@@ -93,19 +93,48 @@ __device__ __forceinline__ void cell_mask_word(const PixelwiseArgs &a, const PwS
     // the cell's lambda pixel, clamped to the plane (cell_pixel); cell coordinates stay far inside int,
     // so the clamp is done on floats and the conversion is a 32-bit one
     const int ix = (int)fminf(fmaxf(floorf(FG_FMUL((float)i, a.delta)), 0.0f), (float)(a.in_w - 1));
-    int iy_prev = -1;
-    long long thresh = 0;
+    auto iy_of = [&](int j) {
+        return (int)fminf(fmaxf(floorf(FG_FMUL((float)j, a.delta)), 0.0f), (float)(a.in_h - 1));
+    };
+    const int jb = g.gj0 + 32 * k;
+    // iy_of is nondecreasing in j (rounding and floor are monotone), so the word's 32 rows take at most
+    // a few pixel rows: one when the first and last agree, two when they differ by one (the boundary
+    // found by bisection); otherwise each row is looked up
+    const int iy0 = iy_of(jb), iy1 = iy_of(jb + 31);
+    const long long t0 = a.cells[(long long)iy0 * a.in_w + ix].thresh;
     unsigned int word = 0;
-#pragma unroll 4
-    for (int r = 0; r < 32; r++) {
-        const int j = g.gj0 + 32 * k + r;
-        const int iy = (int)fminf(fmaxf(floorf(FG_FMUL((float)j, a.delta)), 0.0f), (float)(a.in_h - 1));
-        if (iy != iy_prev) {
-            iy_prev = iy;
-            thresh = a.cells[(long long)iy * a.in_w + ix].thresh;
+    if (iy1 <= iy0 + 1) {
+        int rb = 32;  // first row of pixel row iy1
+        long long t1 = t0;
+        if (iy1 != iy0) {
+            int lo = 1, hi = 31;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (iy_of(jb + mid) == iy1) hi = mid;
+                else lo = mid + 1;
+            }
+            rb = lo;
+            t1 = a.cells[(long long)iy1 * a.in_w + ix].thresh;
         }
-        const long long v = (long long)(small_first_u64(cell_row_hash(colh, j)) >> 11);
-        word |= (v > thresh ? 1u : 0u) << r;
+#pragma unroll 4
+        for (int r = 0; r < 32; r++) {
+            const long long thresh = r < rb ? t0 : t1;
+            const long long v = (long long)(small_first_u64(cell_row_hash(colh, jb + r)) >> 11);
+            word |= (v > thresh ? 1u : 0u) << r;
+        }
+    } else {
+        int iy_prev = iy0;
+        long long thresh = t0;
+#pragma unroll 4
+        for (int r = 0; r < 32; r++) {
+            const int iy = iy_of(jb + r);
+            if (iy != iy_prev) {
+                iy_prev = iy;
+                thresh = a.cells[(long long)iy * a.in_w + ix].thresh;
+            }
+            const long long v = (long long)(small_first_u64(cell_row_hash(colh, jb + r)) >> 11);
+            word |= (v > thresh ? 1u : 0u) << r;
+        }
     }
     cellmask[t] = word;
 }
@@ -117,11 +146,19 @@ __device__ __noinline__ bool sparse_regen_sample(const PixelwiseArgs &a, float x
     return eval_regen(a, U, xg, yg, i0, i1, j0, j1);
 }
 
-// Grain count of cell (i, j) with the stream left after the Poisson draws.
+// Grain count of cell (i, j), which the emptiness bitmask lists as non-empty, with the stream left
+// after the Poisson draws: cell_count_h without its separate first-draw test -- in the Knuth regime the
+// first draw is known to exceed the threshold, so the seeded stream's first output starts the product.
 __device__ __forceinline__ uint32_t sparse_cell_count(const PixelwiseArgs &a, int i, int j, Xoshiro *rng) {
     const CellParam cp = a.cells[cell_pixel(a, i, j)];
-    Xoshiro r;
-    const uint32_t q = cell_count(a.seed, i, j, cp, r);
+    Xoshiro r = small_seed(cell_row_hash(cell_col_hash(a.seed, i), j));
+    uint32_t q;
+    if (cp.thresh >= 0) {
+        q = poisson_knuth_tail(u53_unit(r.next() >> 11), cp.exp_lambda, r);
+    } else {
+        const PoissonParams P = poisson_new(-cp.exp_lambda);
+        q = poisson_rejection(P, r);
+    }
     *rng = r;
     return q;
 }
