@@ -102,40 +102,52 @@ __device__ __forceinline__ void cell_mask_word(const PixelwiseArgs &a, const PwS
     // found by bisection); otherwise each row is looked up
     const int iy0 = iy_of(jb), iy1 = iy_of(jb + 31);
     const long long t0 = a.cells[(long long)iy0 * a.in_w + ix].thresh;
-    unsigned int word = 0;
-    if (iy1 <= iy0 + 1) {
-        int rb = 32;  // first row of pixel row iy1
-        long long t1 = t0;
-        if (iy1 != iy0) {
-            int lo = 1, hi = 31;
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (iy_of(jb + mid) == iy1) hi = mid;
-                else lo = mid + 1;
+    // The row stage of mix3 is fmix64(rotl64(col + j, 41) + phi).  With base = col + jb, when adding
+    // r < 32 carries nothing out of base's low 23 bits, rotl64(base + r, 41) = rotl64(base, 41) + r * 2^41,
+    // so the row hash's input is one constant plus r * 2^41 (only its high word changes); a word whose
+    // rows would carry (31 in 2^23) takes the row hash as is.
+    const uint64_t base = colh + (uint64_t)(int64_t)jb;
+    const uint64_t c0 = rotl64(base, 41) + kPhi;
+    auto scan = [&](auto row_hash) {
+        unsigned int word = 0;
+        if (iy1 <= iy0 + 1) {
+            int rb = 32;  // first row of pixel row iy1
+            long long t1 = t0;
+            if (iy1 != iy0) {
+                int lo = 1, hi = 31;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (iy_of(jb + mid) == iy1) hi = mid;
+                    else lo = mid + 1;
+                }
+                rb = lo;
+                t1 = a.cells[(long long)iy1 * a.in_w + ix].thresh;
             }
-            rb = lo;
-            t1 = a.cells[(long long)iy1 * a.in_w + ix].thresh;
-        }
 #pragma unroll 4
-        for (int r = 0; r < 32; r++) {
-            const long long thresh = r < rb ? t0 : t1;
-            const long long v = (long long)(small_first_u64(cell_row_hash(colh, jb + r)) >> 11);
-            word |= (v > thresh ? 1u : 0u) << r;
-        }
-    } else {
-        int iy_prev = iy0;
-        long long thresh = t0;
-#pragma unroll 4
-        for (int r = 0; r < 32; r++) {
-            const int iy = iy_of(jb + r);
-            if (iy != iy_prev) {
-                iy_prev = iy;
-                thresh = a.cells[(long long)iy * a.in_w + ix].thresh;
+            for (int r = 0; r < 32; r++) {
+                const long long thresh = r < rb ? t0 : t1;
+                const long long v = (long long)(small_first_u64(row_hash(r)) >> 11);
+                word |= (v > thresh ? 1u : 0u) << r;
             }
-            const long long v = (long long)(small_first_u64(cell_row_hash(colh, jb + r)) >> 11);
-            word |= (v > thresh ? 1u : 0u) << r;
+        } else {
+            int iy_prev = iy0;
+            long long thresh = t0;
+#pragma unroll 4
+            for (int r = 0; r < 32; r++) {
+                const int iy = iy_of(jb + r);
+                if (iy != iy_prev) {
+                    iy_prev = iy;
+                    thresh = a.cells[(long long)iy * a.in_w + ix].thresh;
+                }
+                const long long v = (long long)(small_first_u64(row_hash(r)) >> 11);
+                word |= (v > thresh ? 1u : 0u) << r;
+            }
         }
-    }
+        return word;
+    };
+    const unsigned int word = (base & 0x7FFFFFull) <= 0x7FFFFFull - 31
+                                  ? scan([&](int r) { return fmix64(c0 + ((uint64_t)r << 41)); })
+                                  : scan([&](int r) { return cell_row_hash(colh, jb + r); });
     cellmask[t] = word;
 }
 
