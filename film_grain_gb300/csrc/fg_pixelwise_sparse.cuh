@@ -123,11 +123,23 @@ __device__ __forceinline__ void cell_mask_word(const PixelwiseArgs &a, const PwS
                 rb = lo;
                 t1 = a.cells[(long long)iy1 * a.in_w + ix].thresh;
             }
+            // v > thresh for the 53-bit draw v = r1 >> 11 of the first output r1 is r1 - 1 >= m(thresh)
+            // (unsigned) with m = (thresh + 1) * 2^11 - 1, 0 for a negative threshold (always
+            // non-empty), all ones at or above 2^53 - 1 (never).  An all-zero seed (r1 = 0 before
+            // small_seed's remap) wraps to all ones and lists the cell: the sparse pass counts it exactly.
+            auto m_of = [](long long th) -> uint64_t {
+                if (th < 0) return 0ull;
+                if (th >= (1ll << 53) - 1) return ~0ull;
+                return (((uint64_t)th + 1ull) << 11) - 1ull;
+            };
+            const uint64_t m0 = m_of(t0), m1 = m_of(t1);
 #pragma unroll 4
             for (int r = 0; r < 32; r++) {
-                const long long thresh = r < rb ? t0 : t1;
-                const long long v = (long long)(small_first_u64(row_hash(r)) >> 11);
-                word |= (v > thresh ? 1u : 0u) << r;
+                const uint64_t h = row_hash(r);
+                const uint64_t s0 = pcg_pair(pcg_word<1>(h), pcg_word<2>(h));
+                const uint64_t s3 = pcg_pair(pcg_word<7>(h), pcg_word<8>(h));
+                const uint64_t r1m = rotl64(s0 + s3, 23) + s0 - 1ull;
+                word |= (r1m >= (r < rb ? m0 : m1) ? 1u : 0u) << r;
             }
         } else {
             int iy_prev = iy0;
@@ -159,14 +171,17 @@ __device__ __noinline__ bool sparse_regen_sample(const PixelwiseArgs &a, float x
 }
 
 // Grain count of cell (i, j), which the emptiness bitmask lists as non-empty, with the stream left
-// after the Poisson draws: cell_count_h without its separate first-draw test -- in the Knuth regime the
-// first draw is known to exceed the threshold, so the seeded stream's first output starts the product.
+// after the Poisson draws: cell_count_h with the seeded stream's first output as its first draw (no
+// separate first-draw hash).
 __device__ __forceinline__ uint32_t sparse_cell_count(const PixelwiseArgs &a, int i, int j, Xoshiro *rng) {
     const CellParam cp = a.cells[cell_pixel(a, i, j)];
     Xoshiro r = small_seed(cell_row_hash(cell_col_hash(a.seed, i), j));
     uint32_t q;
     if (cp.thresh >= 0) {
-        q = poisson_knuth_tail(u53_unit(r.next() >> 11), cp.exp_lambda, r);
+        // the first draw (above the threshold for every listed cell but one whose seed words 1, 2, 7 and
+        // 8 are all zero, which the bitmask lists to be safe)
+        const uint64_t v = r.next() >> 11;
+        q = (long long)v > cp.thresh ? poisson_knuth_tail(u53_unit(v), cp.exp_lambda, r) : 0u;
     } else {
         const PoissonParams P = poisson_new(-cp.exp_lambda);
         q = poisson_rejection(P, r);
