@@ -132,15 +132,19 @@ __device__ __forceinline__ void cell_mask_word(const PixelwiseArgs &a, const PwS
                 if (th >= (1ll << 53) - 1) return ~0ull;
                 return (((uint64_t)th + 1ull) << 11) - 1ull;
             };
-            const uint64_t m0 = m_of(t0), m1 = m_of(t1);
-#pragma unroll 4
-            for (int r = 0; r < 32; r++) {
+            auto bit = [&](int r, uint64_t m) -> unsigned {
                 const uint64_t h = row_hash(r);
                 const uint64_t s0 = pcg_pair(pcg_word<1>(h), pcg_word<2>(h));
                 const uint64_t s3 = pcg_pair(pcg_word<7>(h), pcg_word<8>(h));
                 const uint64_t r1m = rotl64(s0 + s3, 23) + s0 - 1ull;
-                word |= (r1m >= (r < rb ? m0 : m1) ? 1u : 0u) << r;
-            }
+                return (r1m >= m ? 1u : 0u) << r;
+            };
+            // rows before rb take pixel row iy0's threshold, the others iy1's
+            const uint64_t m0 = m_of(t0), m1 = m_of(t1);
+#pragma unroll 4
+            for (int r = 0; r < rb; r++) word |= bit(r, m0);
+#pragma unroll 4
+            for (int r = rb; r < 32; r++) word |= bit(r, m1);
         } else {
             int iy_prev = iy0;
             long long thresh = t0;
