@@ -159,7 +159,9 @@ __device__ __forceinline__ uint32_t pixelwise_pixel_split(const PixelwiseArgs &a
                 } else {
                     // phase 1
                     mid = ((ni - 1) >> 1) * 8 + ((nj - 1) >> 1);
-                    long long pix = -1, thresh = 0;
+                    // (the screen may pass a cell whose seed words are all zero: phase 2 counts it exactly)
+                    long long pix = -1;
+                    uint64_t bound = 0;
                     for (int di = 0; di < ni; di++) {
                         const int i = i0 + di;
                         const uint64_t colh = cell_col_hash(a.seed, i);
@@ -168,13 +170,11 @@ __device__ __forceinline__ uint32_t pixelwise_pixel_split(const PixelwiseArgs &a
                             const long long p = cell_pixel(a, i, j);
                             if (p != pix) {
                                 pix = p;
-                                thresh = a.cells[p].thresh;
+                                bound = screen_bound(a.cells[p].thresh);
                             }
-                            const uint64_t h = cell_row_hash(colh, j);
-                            const long long v = (long long)(small_first_u64(h) >> 11);
                             const int idx = di * 8 + dj;
                             const int pos = idx == mid ? 0 : (idx == 0 ? mid : idx);
-                            if (v > thresh) m |= 1ull << pos;
+                            if (first_draw_screen(cell_row_hash(colh, j), bound)) m |= 1ull << pos;
                         }
                     }
                 }
@@ -638,8 +638,7 @@ __device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root
                 const int lane = tid & 31;
                 int ci = c0 / (int)Hc, cj = c0 % (int)Hc;
                 int col = -1, pix = -1;
-                uint64_t colh = 0;
-                long long thresh = 0;
+                uint64_t colh = 0, bound = 0;
                 for (int step = 0; step < per; step++) {
                     const int c = c0 + step;
                     bool nonempty = false;
@@ -652,12 +651,11 @@ __device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root
                         const int p = S.rowiy[cj] * a.in_w + S.colix[ci];
                         if (p != pix) {
                             pix = p;
-                            thresh = a.cells[p].thresh;
+                            bound = screen_bound(a.cells[p].thresh);
                         }
-                        const uint64_t h = cell_row_hash(colh, wj0 + cj);
-                        const long long v = (long long)(small_first_u64(h) >> 11);
                         rc = cj * (int)Wc + ci;
-                        nonempty = v > thresh;
+                        // (a cell whose seed words are all zero may pass: A2 counts it exactly)
+                        nonempty = first_draw_screen(cell_row_hash(colh, wj0 + cj), bound);
                         if (!nonempty) S.pre[rc] = 0;
                         if (++cj == (int)Hc) {
                             cj = 0;

@@ -123,24 +123,11 @@ __device__ __forceinline__ void cell_mask_word(const PixelwiseArgs &a, const PwS
                 rb = lo;
                 t1 = a.cells[(long long)iy1 * a.in_w + ix].thresh;
             }
-            // v > thresh for the 53-bit draw v = r1 >> 11 of the first output r1 is r1 - 1 >= m(thresh)
-            // (unsigned) with m = (thresh + 1) * 2^11 - 1, 0 for a negative threshold (always
-            // non-empty), all ones at or above 2^53 - 1 (never).  An all-zero seed (r1 = 0 before
-            // small_seed's remap) wraps to all ones and lists the cell: the sparse pass counts it exactly.
-            auto m_of = [](long long th) -> uint64_t {
-                if (th < 0) return 0ull;
-                if (th >= (1ll << 53) - 1) return ~0ull;
-                return (((uint64_t)th + 1ull) << 11) - 1ull;
-            };
-            auto bit = [&](int r, uint64_t m) -> unsigned {
-                const uint64_t h = row_hash(r);
-                const uint64_t s0 = pcg_pair(pcg_word<1>(h), pcg_word<2>(h));
-                const uint64_t s3 = pcg_pair(pcg_word<7>(h), pcg_word<8>(h));
-                const uint64_t r1m = rotl64(s0 + s3, 23) + s0 - 1ull;
-                return (r1m >= m ? 1u : 0u) << r;
-            };
+            // the first-draw test as first_draw_screen: a cell whose seed words are all zero is listed and
+            // counted exactly by the sparse pass (sparse_cell_count)
+            auto bit = [&](int r, uint64_t m) -> unsigned { return (first_draw_screen(row_hash(r), m) ? 1u : 0u) << r; };
             // rows before rb take pixel row iy0's threshold, the others iy1's
-            const uint64_t m0 = m_of(t0), m1 = m_of(t1);
+            const uint64_t m0 = screen_bound(t0), m1 = screen_bound(t1);
 #pragma unroll 4
             for (int r = 0; r < rb; r++) word |= bit(r, m0);
 #pragma unroll 4

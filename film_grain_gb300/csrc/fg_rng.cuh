@@ -168,6 +168,22 @@ FG_HD uint64_t small_first_u64(uint64_t h) {
     }
     return rotl64(s0 + s3, 23) + s0;
 }
+// The emptiness screen of a cell with hash h: true when its first draw v = small_first_u64(h) >> 11
+// exceeds its Knuth threshold, computed as r1 - 1 >= screen_bound(thresh) (unsigned) on the first
+// output r1 built from seed words 1, 2, 7 and 8 without the all-zero remap -- (thresh + 1) * 2^11 - 1,
+// 0 for a negative threshold (always true), all ones from 2^53 - 1 up (never).  An all-zero seed wraps
+// to true: every caller follows a passing screen with the exact count (cell_count_h), so the wrap costs
+// work, never a result.
+FG_HD uint64_t screen_bound(long long thresh) {
+    if (thresh < 0) return 0ull;
+    if (thresh >= (1ll << 53) - 1) return ~0ull;
+    return (((uint64_t)thresh + 1ull) << 11) - 1ull;
+}
+FG_HD bool first_draw_screen(uint64_t h, uint64_t bound) {
+    const uint64_t s0 = pcg_pair(pcg_word<1>(h), pcg_word<2>(h));
+    const uint64_t s3 = pcg_pair(pcg_word<7>(h), pcg_word<8>(h));
+    return rotl64(s0 + s3, 23) + s0 - 1ull >= bound;
+}
 // src/rng.rs:26-29 / 31-34
 FG_HD Xoshiro cell_rng(uint64_t seed, int32_t i, int32_t j) { return small_seed(mix3(seed, kCellStream, i, j)); }
 FG_HD Xoshiro pixel_rng(uint64_t seed, int32_t i, int32_t j) { return small_seed(mix3(seed, kPixelStream, i, j)); }
