@@ -43,3 +43,14 @@ def test_library_small_rng_seeding_matches_rand_core_default(tmp_path):
         st = (st + 0x9E3779B97F4A7C15) & M64
         zero.append(_splitmix_py(st - 0x9E3779B97F4A7C15 & M64))
     assert [int(t) for t in out[-1].split()] == zero
+
+
+def test_bitmask_screen_and_row_hash_identities(tmp_path):
+    """The sparse pass's emptiness bitmask: the one-compare first-draw screen agrees with the draw's own
+    threshold test on every threshold around each draw and at the edges, and a word's row-hash inputs
+    are one rotated constant plus r * 2^41 when the rows carry nothing out of the low 23 bits."""
+    exe = _compile("screen_check.cpp", "screen_check", tmp_path)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    checked, bad, checked2, bad2 = (int(v) for v in out)
+    assert checked == 200000 * 13 and bad == 0
+    assert checked2 > 6000000 and bad2 == 0
