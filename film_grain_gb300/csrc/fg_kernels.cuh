@@ -79,6 +79,11 @@ struct PixelwiseArgs {
     float radius_mean;
     double log_mu, log_sigma;
     int *cancel;                // null, or the in-launch cancellation words (cancel_requested)
+    // null, or the plane's emptiness bitmask (the sparse pass's first_draw_screen of every cell):
+    // cells [cm_gi0, cm_gi0 + cm_gw) x [cm_gj0, cm_gj0 + 32 cm_ghw), word (c, k) = cellmask[k * cm_gw + c]
+    // holding rows cm_gj0 + 32k .. + 31 of column cm_gi0 + c
+    const unsigned int *cellmask;
+    int cm_gi0, cm_gj0, cm_gw, cm_ghw;
 };
 
 constexpr int kGwBucketCount = 256;  // bucket index over the frac(offx)-sorted offsets

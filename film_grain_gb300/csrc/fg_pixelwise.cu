@@ -263,7 +263,8 @@ cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, unsign
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     PwSparseGrid g;
-    if (cellmask && plan_sparse(a, nby, sms, &g)) {
+    const bool sparse = cellmask && plan_sparse(a, nby, sms, &g);
+    if (sparse) {
         g.cellmask = cellmask;
         const long long words = (long long)g.gw * g.ghw;
         cell_mask_kernel<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(a, g, cellmask);
@@ -281,7 +282,15 @@ cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, unsign
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const long long grid = std::min<long long>(nblocks, (long long)std::max(1, sms) * PwFat::kCtasPerSm);
-    pixelwise_deferred_kernel<<<(unsigned)grid, PwFat::kThreads, fat_smem, s>>>(a, defer + 1);
+    PixelwiseArgs ad = a;  // after the sparse pass, the fat pass reads cell emptiness from its bitmask
+    if (sparse) {
+        ad.cellmask = cellmask;
+        ad.cm_gi0 = g.gi0;
+        ad.cm_gj0 = g.gj0;
+        ad.cm_gw = g.gw;
+        ad.cm_ghw = g.ghw;
+    }
+    pixelwise_deferred_kernel<<<(unsigned)grid, PwFat::kThreads, fat_smem, s>>>(ad, defer + 1);
     return cudaGetLastError();
 }
 

@@ -630,8 +630,10 @@ __device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root
             // ---- pass A1: which window cells hold grains.  The first uniform alone decides q == 0
             // (cell_count_h), so every cell costs the same; each thread walks a contiguous run of cells
             // in column-major order, reusing the column stage of the cell hash and the lambda pixel's
-            // Poisson set-up along the run.  Empty cells get count 0; the others join the list
-            // (one shared atomic per warp step) and get their count in A2.
+            // Poisson set-up along the run -- or, when the plane's emptiness bitmask covers the window
+            // (blocks the sparse pass left to this one), reading the cells' bits from it.  Empty cells
+            // get count 0; the others join the list (one shared atomic per warp step) and get their
+            // count in A2.
             {
                 const int per = (nc + nthreads - 1) / nthreads;
                 const int c0 = tid * per, c1 = min(nc, c0 + per);
@@ -639,23 +641,38 @@ __device__ __forceinline__ bool pixelwise_block(const PixelwiseArgs &a, int root
                 int ci = c0 / (int)Hc, cj = c0 % (int)Hc;
                 int col = -1, pix = -1;
                 uint64_t colh = 0, bound = 0;
+                const bool from_mask = a.cellmask != nullptr && wi0 >= a.cm_gi0 &&
+                                       wi0 + (int)Wc <= a.cm_gi0 + a.cm_gw && wj0 >= a.cm_gj0 &&
+                                       wj0 + (int)Hc <= a.cm_gj0 + 32 * a.cm_ghw;
+                long long mword_at = -1;
+                unsigned mword = 0u;
                 for (int step = 0; step < per; step++) {
                     const int c = c0 + step;
                     bool nonempty = false;
                     int rc = 0;
                     if (c < c1) {
-                        if (ci != col) {
-                            col = ci;
-                            colh = cell_col_hash(a.seed, wi0 + ci);
-                        }
-                        const int p = S.rowiy[cj] * a.in_w + S.colix[ci];
-                        if (p != pix) {
-                            pix = p;
-                            bound = screen_bound(a.cells[p].thresh);
-                        }
                         rc = cj * (int)Wc + ci;
+                        if (from_mask) {
+                            const int gr = wj0 + cj - a.cm_gj0;
+                            const long long at = (long long)(gr >> 5) * a.cm_gw + (wi0 + ci - a.cm_gi0);
+                            if (at != mword_at) {
+                                mword_at = at;
+                                mword = __ldg(a.cellmask + at);
+                            }
+                            nonempty = ((mword >> (gr & 31)) & 1u) != 0u;
+                        } else {
+                            if (ci != col) {
+                                col = ci;
+                                colh = cell_col_hash(a.seed, wi0 + ci);
+                            }
+                            const int p = S.rowiy[cj] * a.in_w + S.colix[ci];
+                            if (p != pix) {
+                                pix = p;
+                                bound = screen_bound(a.cells[p].thresh);
+                            }
+                            nonempty = first_draw_screen(cell_row_hash(colh, wj0 + cj), bound);
+                        }
                         // (a cell whose seed words are all zero may pass: A2 counts it exactly)
-                        nonempty = first_draw_screen(cell_row_hash(colh, wj0 + cj), bound);
                         if (!nonempty) S.pre[rc] = 0;
                         if (++cj == (int)Hc) {
                             cj = 0;
