@@ -31,7 +31,7 @@ __all__ = [
     "RadiusDist", "Algo", "ColorMode", "MaxRadius", "Roi", "ParamsBuilder", "Params", "Derived", "RenderStats",
     "RenderError", "ParamsError", "CancelledError", "GpuError", "derive_common", "default_cell_delta",
     "normalize_plane", "lambda_plane", "lambda_from_plane", "choose_algorithm", "render_pixelwise", "render_grainwise",
-    "render_with_input_image", "dry_run_with_input_image", "lib", "pixelwise_diagnostics", "pixelwise_kernel_count",
+    "render_with_input_image", "dry_run_with_input_image", "lib", "pixelwise_diagnostics", "pixelwise_sparse_forms", "pixelwise_kernel_count",
     "make_offsets",
     "Batch", "BatchTuning",
 ]
@@ -182,6 +182,7 @@ SIGNATURES = {
     "fg_last_error_message": (ctypes.c_char_p, []),
     "fg_version": (ctypes.c_char_p, []),
     "fg_pixelwise_diagnostics": (None, [_P(ctypes.c_ulonglong)]),
+    "fg_pixelwise_sparse_forms": (None, [_P(ctypes.c_ulonglong)]),
     "fg_pixelwise_kernel_count": (ctypes.c_int, [_P(_ParamsC), _P(_DerivedC), ctypes.c_void_p, _P(ctypes.c_int32)]),
     "fg_batch_create": (ctypes.c_int, [_P(_BatchImageC), ctypes.c_int32, _P(BatchTuning), _P(ctypes.c_void_p)]),
     "fg_batch_run": (ctypes.c_int, [ctypes.c_void_p, _vp]),
@@ -459,8 +460,9 @@ def render_grainwise(lam, params: Params, derived: Derived, cancel: Optional[Cal
 
 
 def pixelwise_kernel_count(params: "Params", derived: "Derived") -> int:
-    """Kernel launches one pixel-wise render of these params makes: 3 on the per-sample kernel, 5 on the
-    sparse block pass (with the plane's emptiness bitmask), 4 on the lean block pass."""
+    """Kernel launches one pixel-wise render of these params makes: 3 on the per-sample kernel, 6 on the
+    sparse block pass (with the plane's emptiness bitmask and the sorted offsets), 4 on the lean block
+    pass."""
     offs = np.ascontiguousarray(derived.offsets_input, np.float32)
     n = ctypes.c_int32()
     _raise(lib().fg_pixelwise_kernel_count(params.c, derived._c, offs.ctypes.data, ctypes.byref(n)))
@@ -472,6 +474,14 @@ def pixelwise_diagnostics() -> Tuple[int, int, int, int]:
     thread's last pixel-wise render."""
     arr = (ctypes.c_ulonglong * 4)()
     lib().fg_pixelwise_diagnostics(arr)
+    return tuple(int(v) for v in arr)
+
+
+def pixelwise_sparse_forms() -> Tuple[int, int]:
+    """(sample-major, grain-major) blocks of the sparse block pass in this thread's last pixel-wise
+    render: the two forms of its sample step, which give identical counts."""
+    arr = (ctypes.c_ulonglong * 2)()
+    lib().fg_pixelwise_sparse_forms(arr)
     return tuple(int(v) for v in arr)
 
 

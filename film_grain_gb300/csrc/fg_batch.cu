@@ -315,15 +315,15 @@ static fg_status batch_build(const fg_batch_image *imgs, int n, const fg_batch_t
             FG_BCUDA(dev_alloc(b, sizeof(float) * 2 * p.n_samples, &d_offs), "batch alloc");
             FG_BCUDA(cudaMemcpy(d_offs, im.offsets, sizeof(float) * 2 * p.n_samples, cudaMemcpyHostToDevice), "H2D");
             FG_BCUDA(dev_alloc(b, sizeof(CellParam) * n_in, &d_cells), "batch alloc");
-            FG_BCUDA(dev_alloc(b, sizeof(unsigned long long) * 4, &d_diag), "batch alloc");
+            FG_BCUDA(dev_alloc(b, sizeof(unsigned long long) * kPwDiagWords, &d_diag), "batch alloc");
             const PwPlan pl = plan_pixelwise(p, d, im.offsets, tun.pixel_max_block_log2);
             PixelwiseArgs &a = B.pa;
             a = pixelwise_args(p, d, pl, im.d_lambda, (const CellParam *)d_cells, (const float *)d_offs, im.d_out,
                                (unsigned long long *)d_diag);
             segs.push_back(Segment{0, 0, n_out, im.d_out, nullptr, 0.0f});
             add_chunks(pre, (int)segs.size() - 1, n_out);
-            segs.push_back(Segment{0, 0, 4 * 2, d_diag, nullptr, 0.0f});
-            add_chunks(pre, (int)segs.size() - 1, 8);
+            segs.push_back(Segment{0, 0, kPwDiagWords * 2, d_diag, nullptr, 0.0f});
+            add_chunks(pre, (int)segs.size() - 1, kPwDiagWords * 2);
             segs.push_back(Segment{1, 0, n_in, (void *)im.d_lambda, d_cells, d.delta});
             add_chunks(pre, (int)segs.size() - 1, n_in);
             segs.push_back(Segment{2, 0, n_out, im.d_out, nullptr, 1.0f / (float)p.n_samples});

@@ -20,7 +20,7 @@
 
 namespace fg {
 
-static thread_local unsigned long long g_pw_diag[4] = {0, 0, 0, 0};
+static thread_local unsigned long long g_pw_diag[kPwDiagWords] = {0, 0, 0, 0, 0, 0};
 
 fg_status cuda_error(cudaError_t e, const char *what) {
     return set_error(e == cudaErrorMemoryAllocation ? FG_ERR_NOMEM : FG_ERR_CUDA,
@@ -444,8 +444,8 @@ static fg_status render_plane_sync(int algo, const float *lambda, const fg_param
     }
     if (algo == FG_ALGO_PIXEL) {
         FG_CUDA(b_cells.alloc(sizeof(CellParam) * n_in, s), "alloc cell table");
-        FG_CUDA(b_diag.alloc(sizeof(unsigned long long) * 4, s), "alloc diag");
-        FG_CUDA(cudaMemsetAsync(b_diag.p, 0, sizeof(unsigned long long) * 4, s), "memset diag");
+        FG_CUDA(b_diag.alloc(sizeof(unsigned long long) * kPwDiagWords, s), "alloc diag");
+        FG_CUDA(cudaMemsetAsync(b_diag.p, 0, sizeof(unsigned long long) * kPwDiagWords, s), "memset diag");
         st = enqueue_pixelwise(d_lam, p, d, h_offs.data(), d_offs, d_out, (CellParam *)b_cells.p,
                                (unsigned long long *)b_diag.p, nullptr, s, true, watch.dev());
     } else {
@@ -499,8 +499,8 @@ FG_API fg_status fg_render_pixelwise_async(const float *d_lambda, const fg_param
     FG_CUDA(b_offs.alloc(off_bytes, s), "alloc offsets");
     FG_CUDA(cudaMemcpyAsync(b_offs.p, offsets_input, off_bytes, cudaMemcpyHostToDevice, s), "offsets H2D");
     FG_CUDA(b_cells.alloc(sizeof(CellParam) * n_in, s), "alloc cell table");
-    FG_CUDA(b_diag.alloc(sizeof(unsigned long long) * 4, s), "alloc diag");
-    FG_CUDA(cudaMemsetAsync(b_diag.p, 0, sizeof(unsigned long long) * 4, s), "memset diag");
+    FG_CUDA(b_diag.alloc(sizeof(unsigned long long) * kPwDiagWords, s), "alloc diag");
+    FG_CUDA(cudaMemsetAsync(b_diag.p, 0, sizeof(unsigned long long) * kPwDiagWords, s), "memset diag");
     return enqueue_pixelwise(d_lambda, *params, *derived, offsets_input, (const float *)b_offs.p, d_out,
                              (CellParam *)b_cells.p, (unsigned long long *)b_diag.p, nullptr, s);
 }
@@ -593,8 +593,8 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
     const size_t mask_bytes = algo == FG_ALGO_GRAIN ? grainwise_mask_bytes(p, d) : 0;
     if (algo == FG_ALGO_PIXEL) {
         FG_CUDA(b_cells.alloc(sizeof(CellParam) * n_in, s), "alloc cell table");
-        FG_CUDA(b_diag.alloc(sizeof(unsigned long long) * 4, s), "alloc diag");
-        FG_CUDA(cudaMemsetAsync(b_diag.p, 0, sizeof(unsigned long long) * 4, s), "memset diag");
+        FG_CUDA(b_diag.alloc(sizeof(unsigned long long) * kPwDiagWords, s), "alloc diag");
+        FG_CUDA(cudaMemsetAsync(b_diag.p, 0, sizeof(unsigned long long) * kPwDiagWords, s), "memset diag");
     } else {
         FG_CUDA(b_cells.alloc(mask_bytes * nplanes, s), "alloc sample masks");
     }
@@ -641,6 +641,12 @@ FG_API fg_status fg_render_image(const float *rgb, int64_t width, int64_t height
 // per-sample regeneration path, blocks without a staged window, block subdivisions, blocks run.
 FG_API void fg_pixelwise_diagnostics(unsigned long long out[4]) {
     for (int i = 0; i < 4; i++) out[i] = g_pw_diag[i];
+}
+
+// The sparse pass's blocks of that render by the form of their sample step: sample-major, grain-major.
+FG_API void fg_pixelwise_sparse_forms(unsigned long long out[2]) {
+    out[0] = g_pw_diag[4];
+    out[1] = g_pw_diag[5];
 }
 
 FG_API fg_status fg_pixelwise_kernel_count(const fg_params *params, const fg_derived *derived,

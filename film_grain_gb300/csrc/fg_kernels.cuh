@@ -33,6 +33,10 @@ constexpr int kPwEdgeMax = 128;    // window cells per axis
 constexpr int kPwKChunk = 256;     // offsets per sample-assignment chunk
 constexpr int kPwFootMax = 1024;   // per-block output-pixel counters
 constexpr int kPwMaxLevel = 3;     // block subdivision depth on grain overflow
+// Pixel-wise diagnostic counters (PixelwiseArgs::diag): [0] samples evaluated on the per-sample path,
+// [1] blocks without a staged window, [2] block subdivisions, [3] blocks run, [4] sparse blocks whose
+// samples ran sample-major, [5] sparse blocks that ran grain-major.
+constexpr int kPwDiagWords = 6;
 // A block regenerates per sample (no staging) when its samples' reach, in cells, is below
 // kPwRegenSparse x its window's cells, or below kPwRegenOverflow x them once the window overflows
 // with more than kPwRegenDense of its cells non-empty.

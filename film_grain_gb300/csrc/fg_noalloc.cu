@@ -5,7 +5,7 @@
 // afford cudaMalloc/cudaFree (which can block on the device and take driver locks) in the middle of
 // a frame.  fg_render_pixelwise_noalloc serves them: the caller passes the lambda plane and the
 // output plane (device memory); the kernel's scratch -- the per-input-pixel cell table, the device
-// copy of the offsets and four diagnostic counters -- lives in one file-scope __device__ array of
+// copy of the offsets and the diagnostic counters -- lives in one file-scope __device__ array of
 // fixed size, so nothing is allocated at call time.  The array exists on every GPU that loads this
 // library, from load until process exit.
 //
@@ -30,7 +30,7 @@ namespace fg {
 
 constexpr size_t kNaCellsBytes = (size_t)FG_NOALLOC_MAX_INPUT_PIXELS * sizeof(CellParam);
 constexpr size_t kNaOffsBytes = (size_t)FG_NOALLOC_MAX_SAMPLES * 2 * sizeof(float);
-constexpr size_t kNaDiagBytes = 4 * sizeof(unsigned long long);
+constexpr size_t kNaDiagBytes = kPwDiagWords * sizeof(unsigned long long);
 constexpr size_t kNaScratchBytes = kNaCellsBytes + kNaOffsBytes + kNaDiagBytes;
 
 // The shared scratch of every fg_render_pixelwise_noalloc call on a device.

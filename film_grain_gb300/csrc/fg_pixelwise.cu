@@ -85,20 +85,32 @@ __global__ void __launch_bounds__(C::kThreads, C::kCtasPerSm)
 __global__ void __launch_bounds__(PwSparse::kThreads, PwSparse::kCtasPerSm)
     pixelwise_sparse_kernel(const __grid_constant__ PixelwiseArgs a, const PwSparseGrid g, int nby,
                             int *__restrict__ list) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int sbx = g.sbx0 + (int)(blockIdx.x % (unsigned)g.nsbx), sby = g.sby0 + (int)(blockIdx.x / (unsigned)g.nsbx);
-    pixelwise_sparse_root(a, g, sbx, sby, nby, list, smem_raw);
+    pixelwise_sparse_root(a, g, sbx, sby, nby, list);
 }
 
 // The offsets in ascending x (ties by index: a permutation even with NaNs), for the sparse pass's
-// lanes (sparse_sample_pass).  One CTA; n <= kPwKChunk.
+// lanes (sparse_sample_pass); with gm_ent, also the grain-major form's table of the sorted offsets by
+// phase bin (frac(o.x * zoom), frac(o.y * zoom)): entries bin-major (ties by sorted index), each
+// entry's sorted index, and each bin's first entry (sparse_grain_pass).  One CTA of kPwKChunk threads;
+// n <= kPwKChunk.
 __device__ __forceinline__ unsigned offset_sort_key(float v) {
     const unsigned b = __float_as_uint(v);
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);  // the float order as an unsigned order
 }
-__global__ void __launch_bounds__(256) sort_offsets_kernel(const float2 *__restrict__ offs, int n,
-                                                           float2 *__restrict__ sorted) {
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+__device__ __forceinline__ int offset_phase_bin(float v) {  // v = o * zoom
+    constexpr int B = PwSparse::kGmBins;
+    const float f = v - floorf(v);  // [0, 1]: 1 only when v is just below an integer
+    return min((int)(f * (float)B), B - 1);
+}
+__global__ void __launch_bounds__(kPwKChunk) sort_offsets_kernel(const float2 *__restrict__ offs, int n, float zoom,
+                                                                 float2 *__restrict__ sorted,
+                                                                 float4 *__restrict__ gm_ent, int *__restrict__ gm_idx) {
+    constexpr int B = PwSparse::kGmBins;
+    __shared__ float2 s_sorted[kPwKChunk];
+    __shared__ int s_bin[kPwKChunk];
+    const int k = threadIdx.x;
+    if (k < n) {
         const float2 o = offs[k];
         const unsigned key = offset_sort_key(o.x);
         int rank = 0;
@@ -107,6 +119,29 @@ __global__ void __launch_bounds__(256) sort_offsets_kernel(const float2 *__restr
             rank += (kj < key || (kj == key && j < k)) ? 1 : 0;
         }
         sorted[rank] = o;
+        s_sorted[rank] = o;
+    }
+    if (!gm_ent) return;  // uniform
+    __syncthreads();
+    float4 e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    int bin = 0;
+    if (k < n) {
+        const float2 o = s_sorted[k];
+        e = make_float4(o.x, o.y, o.x * zoom, o.y * zoom);
+        bin = offset_phase_bin(e.w) * B + offset_phase_bin(e.z);
+        s_bin[k] = bin;
+    }
+    __syncthreads();
+    if (k < n) {
+        int pos = 0;
+        for (int j = 0; j < n; j++) pos += (s_bin[j] < bin || (s_bin[j] == bin && j < k)) ? 1 : 0;
+        gm_ent[pos] = e;
+        gm_idx[pos] = k;
+    }
+    for (int b = k; b <= B * B; b += blockDim.x) {
+        int first = 0;
+        for (int j = 0; j < n; j++) first += s_bin[j] < b ? 1 : 0;
+        gm_idx[n + b] = first;
     }
 }
 
@@ -149,6 +184,10 @@ static bool plan_sparse(const PixelwiseArgs &a, int nby, int sms, PwSparseGrid *
         const int gi0 = window_lo((float)sbx0 * bs, a) - 2, gi1 = window_hi((float)(sbx1 + 1) * bs, a) + 2;
         const int gj0 = window_lo((float)sby0 * bs, a) - 2, gj1 = window_hi((float)(sby1 + 1) * bs, a) + 2;
         g->cellmask = nullptr;
+        g->gm_ent = nullptr;
+        g->gm_idx = nullptr;
+        g->gm_eps = g->gm_grain_cost = g->gm_sample_cost = 0.0f;
+        g->gm_noslow = 0;
         g->gi0 = gi0;
         g->gj0 = gj0;
         g->gw = gi1 - gi0 + 1;
@@ -168,9 +207,15 @@ static int sm_count() {
     return sms;
 }
 
-// The sparse pass's scratch: the bitmask, then (16-byte aligned) the offsets sorted by x.
-static size_t sparse_mask_bytes(const PwSparseGrid &g) {
-    return ((size_t)g.gw * g.ghw * sizeof(unsigned int) + 15) & ~(size_t)15;
+// The sparse pass's scratch, each part 16-byte aligned: the bitmask, the offsets sorted by x, the
+// grain-major form's entries (float4) and its index (entry offsets, then bin starts).
+static size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+static size_t sparse_mask_bytes(const PwSparseGrid &g) { return align16((size_t)g.gw * g.ghw * sizeof(unsigned int)); }
+static size_t sparse_gm_ent_at(const PwSparseGrid &g, int n) {
+    return sparse_mask_bytes(g) + align16((size_t)n * sizeof(float2));
+}
+static size_t sparse_gm_idx_at(const PwSparseGrid &g, int n) {
+    return sparse_gm_ent_at(g, n) + (size_t)n * sizeof(float4);
 }
 
 size_t pixelwise_cellmask_bytes(const PixelwiseArgs &a, int nby) {
@@ -178,7 +223,35 @@ size_t pixelwise_cellmask_bytes(const PixelwiseArgs &a, int nby) {
     PwSparseGrid g;
     const int sms = sm_count();  // without a device (planning only): the GB300's 152
     if (!plan_sparse(a, nby, sms > 0 ? sms : 152, &g)) return 0;
-    return sparse_mask_bytes(g) + (size_t)a.n * sizeof(float2);
+    const int bins = PwSparse::kGmBins * PwSparse::kGmBins;
+    return sparse_gm_idx_at(g, a.n) + (size_t)(a.n + bins + 1) * sizeof(int);
+}
+
+// The grain-major form's plane conditions and cost model (sparse_grain_pass).  A grain reaches at most
+// rm * zoom output pixels; the candidate pixel of an offset is exact while that reach plus the f32
+// rounding of the pixel coordinates (eps: a few ulps of the largest coordinate) stays below half a
+// pixel, and the rounding to an integer by adding 1.5 * 2^23 needs coordinates below 2^22.  Costs, in
+// units fitted to timings of both forms (4096^2 planes at r 0.025 log-normal N 256, where grain-major
+// is 20 % faster, and the 256^2 ramp at r 0.12 N 64, where it is 20 % slower): a grain pays its
+// set-up and, per candidate, a disk test and its share of the listed hits, for n (2 (r_mean zoom +
+// eps) + 1/bins)^2 candidates on average; a sample pays the scan of its cell range's columns.
+static bool plan_grain_major(const PixelwiseArgs &a, PwSparseGrid *g) {
+    const double ext = std::max({std::fabs(a.offx_min), std::fabs(a.offx_max), std::fabs(a.offy_min),
+                                 std::fabs(a.offy_max)});
+    const double coord = (double)std::max(a.out_w, a.out_h) + ext * a.zoom + 2.0;
+    const double eps = coord * 0x1p-21 + 0x1p-20;
+    g->gm_eps = (float)eps;
+    const double reach = (double)a.rm * a.zoom;
+    if (!(coord < 0x1p21) || !(reach + eps <= 0.4)) return false;
+    // a sample's range spans floor((xg + rm) / delta) - floor((xg - rm) / delta) cells: 2 rm / delta + 1
+    // and the rounding of xg +- rm and of the divisions (a few ulps of the largest grid coordinate)
+    const double grid = (double)std::max(a.out_w, a.out_h) * a.inv_zoom + ext + a.rm + 2.0;
+    const double span = 2.0 * a.rm / a.delta + 1.0 + 8.0 * grid * 0x1p-23 / a.delta;
+    g->gm_noslow = span <= 30.0 ? 1 : 0;
+    const double band = 2.0 * ((double)a.radius_mean * a.zoom + eps) + 1.0 / PwSparse::kGmBins;
+    g->gm_grain_cost = (float)(120.0 + 60.0 * a.n * band * band);
+    g->gm_sample_cost = (float)(40.0 + 9.0 * (2.0 * a.rm / a.delta + 1.0));
+    return true;
 }
 
 // The root blocks the lean pass deferred, in fat CTAs: persistent, each CTA taking the next listed
@@ -269,8 +342,17 @@ cudaError_t launch_pixelwise(const PixelwiseArgs &a, int nby, int *defer, unsign
         const long long words = (long long)g.gw * g.ghw;
         cell_mask_kernel<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(a, g, cellmask);
         PixelwiseArgs as = a;  // the sparse pass reads the offsets sorted by x
-        as.offs = reinterpret_cast<const float2 *>(reinterpret_cast<char *>(cellmask) + sparse_mask_bytes(g));
-        sort_offsets_kernel<<<1, 256, 0, s>>>(a.offs, a.n, const_cast<float2 *>(as.offs));
+        char *scratch = reinterpret_cast<char *>(cellmask);
+        as.offs = reinterpret_cast<const float2 *>(scratch + sparse_mask_bytes(g));
+        float4 *gm_ent = nullptr;
+        int *gm_idx = nullptr;
+        if (plan_grain_major(a, &g)) {
+            gm_ent = reinterpret_cast<float4 *>(scratch + sparse_gm_ent_at(g, a.n));
+            gm_idx = reinterpret_cast<int *>(scratch + sparse_gm_idx_at(g, a.n));
+            g.gm_ent = gm_ent;
+            g.gm_idx = gm_idx;
+        }
+        sort_offsets_kernel<<<1, kPwKChunk, 0, s>>>(a.offs, a.n, a.zoom, const_cast<float2 *>(as.offs), gm_ent, gm_idx);
         const size_t sparse_smem = sizeof(PwSparseShared);
         e = set_smem(pixelwise_sparse_kernel, sparse_smem);
         if (e != cudaSuccess) return e;

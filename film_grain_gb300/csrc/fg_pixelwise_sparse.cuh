@@ -15,11 +15,15 @@
 //   2. the set bits, ranked in column-major order, list the non-empty cells; their grain counts (the
 //      Poisson draws of src/pixelwise.rs:77-82) are prefix-summed into a CSR over the list and their
 //      grains (centre, radius^2) regenerated into shared memory;
-//   3. each thread takes the owned pixels of one offset (or a share of them) and runs the reference's
-//      per-sample test: for each cell column i0..i1 of the sample's range (src/pixelwise.rs:55-58), the
-//      bits of rows j0..j1 are cut from the mask, and when any is set their grains -- contiguous in
-//      the CSR, since cells of one column follow each other in the list -- get the disk test
-//      dx*dx + dy*dy <= r*r (src/pixelwise.rs:96-99);
+//   3. sample-major: each thread takes the owned pixels of one offset (or a share of them) and runs the
+//      reference's per-sample test: for each cell column i0..i1 of the sample's range
+//      (src/pixelwise.rs:55-58), the bits of rows j0..j1 are cut from the mask, and when any is set
+//      their grains -- contiguous in the CSR, since cells of one column follow each other in the list
+//      -- get the disk test dx*dx + dy*dy <= r*r (src/pixelwise.rs:96-99);
+//      or grain-major (sparse_grain_pass), when a grain's reach is below half an output pixel and the
+//      cost model favours it: each thread takes staged grains, finds the few owned samples within a
+//      grain's radius through a table of the offsets binned by their phase, gives them the same disk
+//      test, and sets a bit per covered sample whose range holds the grain's cell;
 //   4. hit counts go to per-pixel shared counters, then to the output plane (integers, exact in f32).
 // The indicator is an OR over the grains of the sample's cells, so the result equals the reference's
 // early-exit loop bit for bit.
@@ -35,6 +39,9 @@ struct PwSparse {
     static constexpr int kMaskWords = 1280;  // window bitmask, columns an odd number of words apart
     static constexpr int kRowsMax = 256;     // window rows
     static constexpr int kRangeSlots = 4;    // tabulated cell ranges per offset and axis
+    static constexpr int kGmBins = 16;       // phase bins per axis of the grain-major form's offset table
+    static constexpr int kGmBitsWords = 1024;  // owned-sample bits of the grain-major form
+    static constexpr int kGmHitMax = 3584;     // disk tests passed, listed for the hits' pass
 };
 
 // Mask words per window column in shared memory: the column's words rounded up to an odd count, so
@@ -52,12 +59,29 @@ __device__ __forceinline__ unsigned sparse_range_code(float g, float rm, float d
     return (unsigned)(c0 - w0) | ((unsigned)(c1 - c0) << 11);
 }
 
-struct PwSparseShared {
-    float4 grains[PwSparse::kGrainMax];
+// The window's cells (steps 1 and 2, and step 3 in the sample-major form).
+struct PwSparseWindow {
     uint2 mask2[PwSparse::kMaskWords];           // (word w, the next word of the same column or 0)
     unsigned short wrank[PwSparse::kMaskWords];  // non-empty cells before each mask word (column-major)
     unsigned short list[PwSparse::kListMax];     // non-empty cells: window index i * Hc + j, column-major
     unsigned int gsc[PwSparse::kListMax];        // per listed cell: first grain | grain count << 16
+};
+// Step 3 in the grain-major form (sparse_grain_major), written once the window's cells are read.
+struct PwSparseGrainMajor {
+    float4 ent[kPwKChunk];                       // the offsets by phase bin: o.x, o.y, o.x * zoom, o.y * zoom
+    unsigned short k[kPwKChunk];                 // the entry's offset (index into the x-sorted offsets)
+    unsigned short start[PwSparse::kGmBins * PwSparse::kGmBins + 8];  // first entry of each bin, then n
+    int base[kPwKChunk];                         // first bit of each offset's owned samples
+    unsigned int bits[PwSparse::kGmBitsWords];   // one per owned sample: covered by a grain already
+    unsigned int hits[PwSparse::kGmHitMax];      // (grain, entry) pairs that passed the disk test
+};
+
+struct PwSparseShared {
+    float4 grains[PwSparse::kGrainMax];          // centre, r^2, window cell (i - wi0) | (j - wj0) << 16 as bits
+    union {
+        PwSparseWindow w;
+        PwSparseGrainMajor gm;
+    };
     int4 rect[kPwKChunk];                       // owned pixel rectangle per offset: xa, xe, ya, ye
     // cell ranges (sparse_range_code) of the first kRangeSlots columns and rows of each offset's
     // rectangle: entry [slot * n + k]
@@ -68,9 +92,21 @@ struct PwSparseShared {
                                                 // column stored hs = sparse_col_stride(hw) words apart
     int fx0, fx1, fy0, fy1, nsamples;           // owned-pixel footprint, owned samples
     int rw_min, rw_max, rh_min, rh_max;         // extremes of the offsets' rectangle widths and heights
-    int stop, ngrains;
+    int stop, ngrains, any_slow;                // any_slow: a tabulated range code is kRangeSlow
+    int nhits;                                  // disk tests passed in the grain-major form
     float est_grains, est_cells;
 };
+
+static_assert(sizeof(PwSparseGrainMajor) <= sizeof(PwSparseWindow), "the grain-major tables fit the window's space");
+static_assert(PwSparse::kGrainMax <= 2048, "a listed hit holds the grain in 11 bits");
+
+// The CTA's PwSparseShared: the start of its dynamic shared memory, named through the shared array
+// itself, so that the out-of-line functions below address it as shared memory (a reference passed in
+// would reach them as a generic address).
+__device__ __forceinline__ PwSparseShared &sparse_smem() {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    return *reinterpret_cast<PwSparseShared *>(smem_raw);
+}
 
 // Geometry of the sparse pass: block edge `bs` (input pixels) = ratio x the fat grid's edge, block grid
 // origin and width (the fat grid is (a.bx0, a.by0, a.nbx) with a.bsize); and the plane's emptiness
@@ -82,6 +118,12 @@ struct PwSparseGrid {
     int sbx0, sby0, nsbx, nsby;
     const unsigned int *cellmask;
     int gi0, gj0, gw, ghw;
+    // the grain-major form of step 3 (sparse_grain_major); gm_ent null when the plane does not allow it
+    const float4 *gm_ent;   // [n] the x-sorted offsets by phase bin (PwSparseGrainMajor::ent)
+    const int *gm_idx;      // [n] each entry's offset, then [kGmBins^2 + 1] each bin's first entry
+    float gm_eps;           // rounding margin of a grain's phase band, in output pixels
+    int gm_noslow;          // no sample's cell range can span more than 32 cells (none leaves its window)
+    float gm_grain_cost, gm_sample_cost;  // modelled instructions per staged grain / per owned sample
 };
 
 // The plane's emptiness bitmask (step 0): thread t = (word row k = t / gw, column c = t % gw).
@@ -206,18 +248,18 @@ __device__ __forceinline__ int sparse_sample_hit(const PwSparseShared &S, float 
     const int w0 = c0 * hs + (r0 >> 5);
     unsigned cols = 0u;
     for (int i = 0; i <= ncol; i++) {
-        const uint2 m = S.mask2[w0 + i * hs];
+        const uint2 m = S.w.mask2[w0 + i * hs];
         cols |= ((__funnelshift_r(m.x, m.y, b0) & keep) != 0u ? 1u : 0u) << i;
     }
     while (cols) {
         const int w = w0 + (__ffs(cols) - 1) * hs;
         cols &= cols - 1u;
-        const uint2 m = S.mask2[w];
+        const uint2 m = S.w.mask2[w];
         unsigned bits = __funnelshift_r(m.x, m.y, b0) & keep;
-        int rank = S.wrank[w] + __popc(m.x & below);
+        int rank = S.w.wrank[w] + __popc(m.x & below);
         do {  // the column's non-empty cells of the range, in row order
             bits &= bits - 1u;
-            const unsigned sc = S.gsc[rank++];
+            const unsigned sc = S.w.gsc[rank++];
             const int g0 = (int)(sc & 0xFFFFu), ge = g0 + (int)(sc >> 16);
             for (int g = g0; g < ge; g++) {
                 const float4 G = S.grains[g];
@@ -230,8 +272,7 @@ __device__ __forceinline__ int sparse_sample_hit(const PwSparseShared &S, float 
 }
 
 // The second pass over a thread's samples: the ones whose range left the window.
-__device__ __noinline__ void sparse_slow_sample(const PixelwiseArgs &a, PwSparseShared &S, float xg, float yg, int x,
-                                                int y);
+__device__ __noinline__ void sparse_slow_sample(const PixelwiseArgs &a, float xg, float yg, int x, int y);
 
 __device__ __forceinline__ void sparse_count_hit(const PixelwiseArgs &a, PwSparseShared &S, int x, int y) {
     const int fw = S.fx1 - S.fx0, fh = S.fy1 - S.fy0;
@@ -247,7 +288,7 @@ __device__ __forceinline__ void sparse_count_hit(const PixelwiseArgs &a, PwSpars
 // so their mask loads fall on neighbouring columns.  Cell ranges come from the table the ownership pass
 // filled when every rectangle fits it, else they are computed here.
 // One pass over the thread's samples: pass 0 evaluates every sample from the staged window and counts
-// the ones whose range leaves it; pass 1 sends exactly those to the per-sample loop.
+// the ones whose range leaves it; pass 1 sends exactly those to the per-sample loop (and counts them).
 template <int kPass>
 __device__ __forceinline__ unsigned sparse_sample_pass(const PixelwiseArgs &a, PwSparseShared &S) {
     using C = PwSparse;
@@ -273,7 +314,8 @@ __device__ __forceinline__ unsigned sparse_sample_pass(const PixelwiseArgs &a, P
                     if (out) slow++;
                     else if (sparse_sample_hit(S, xg, yg, rx, ry)) sparse_count_hit(a, S, x, y);
                 } else if (out) {
-                    sparse_slow_sample(a, S, xg, yg, x, y);
+                    slow++;
+                    sparse_slow_sample(a, xg, yg, x, y);
                 }
             }
         }
@@ -281,7 +323,8 @@ __device__ __forceinline__ unsigned sparse_sample_pass(const PixelwiseArgs &a, P
     return slow;
 }
 
-__device__ __noinline__ void sparse_samples(const PixelwiseArgs &a, PwSparseShared &S) {
+__device__ __noinline__ void sparse_samples(const PixelwiseArgs &a) {
+    PwSparseShared &S = sparse_smem();
     if (!(a.rm > 0.0f)) return;  // a grain radius is at most rm: nothing can cover a sample
     const unsigned slow = sparse_sample_pass<0>(a, S);
     if (__syncthreads_or(slow != 0)) {
@@ -290,8 +333,136 @@ __device__ __noinline__ void sparse_samples(const PixelwiseArgs &a, PwSparseShar
     }
 }
 
-__device__ __noinline__ void sparse_slow_sample(const PixelwiseArgs &a, PwSparseShared &S, float xg, float yg, int x,
-                                                int y) {
+// A disk test of the grain-major form passed: grain (window cell `cell`) covers the sample of offset
+// k at pixel (rx, ry).  The sample counts when this block owns it, its cell ranges lie inside the
+// window (else pass 1 decides it), the grain's cell lies in its ranges -- the cells the reference
+// visits for it (src/pixelwise.rs:55-58) -- and no other grain covered it before.  The ranges come
+// from the table, or beyond its slots are computed as the table's entries are.
+__device__ __forceinline__ void sparse_gm_hit(const PixelwiseArgs &a, PwSparseShared &S, int k, unsigned cell, float rx,
+                                              float ry) {
+    using C = PwSparse;
+    const int x = (int)rx, y = (int)ry;
+    const int4 R = S.rect[k];
+    if (x < R.x || x >= R.y || y < R.z || y >= R.w) return;  // another block's sample
+    const int sx = x - R.x, sy = y - R.z;
+    const float2 o = a.offs[k];
+    const unsigned cx = sx < C::kRangeSlots ? S.range_x[sx * a.n + k]
+                                            : sparse_range_code(xg_of(x, a.inv_zoom, o.x), a.rm, a.delta, S.wi0, S.wi1);
+    const unsigned cy = sy < C::kRangeSlots ? S.range_y[sy * a.n + k]
+                                            : sparse_range_code(xg_of(y, a.inv_zoom, o.y), a.rm, a.delta, S.wj0, S.wj1);
+    if (cx == kRangeSlow || cy == kRangeSlow) return;
+    if ((cell & 0xFFFFu) - (cx & 0x7FFu) > (cx >> 11) || (cell >> 16) - (cy & 0x7FFu) > (cy >> 11)) return;
+    const int idx = S.gm.base[k] + sy * (R.y - R.x) + sx;
+    const unsigned bit = 1u << (idx & 31);
+    if (!(atomicOr(&S.gm.bits[idx >> 5], bit) & bit)) sparse_count_hit(a, S, x, y);
+}
+
+// Step 3, grain-major: each thread takes staged grains and finds the owned samples within their radius.
+// Sample k of pixel x lies at xg = (x + 0.5) / zoom - o.x, so a grain at gx can cover only the pixel
+// x = rint(gx * zoom - 0.5 + o.x * zoom) of each offset (its reach r * zoom is below half a pixel), and
+// only offsets whose phase frac(o.x * zoom) lies within r * zoom + eps of frac(0.5 - gx * zoom) reach
+// it: the offsets are binned by their two phases (kGmBins^2 bins), and a grain visits the bins its
+// phase band covers.  Every candidate gets the reference's disk test on the reference's xg, yg
+// (src/pixelwise.rs:96-99); the band only has to contain every pixel that can pass it.  A sample's
+// covering grains are OR-ed through its bit, so the count equals the sample-major form's.
+// The pixel coordinate of offset entry O that grain coordinate p = g * zoom - 0.5 can reach, as a float:
+// p + o * zoom rounded to an integer by adding and removing 1.5 * 2^23.
+__device__ __forceinline__ float gm_pixel(float p, float oz) {
+    constexpr float kRint = 12582912.0f;
+    return FG_FSUB(FG_FADD(FG_FADD(p, oz), kRint), kRint);
+}
+
+// A passed disk test is listed as grain | entry << 11 and decided after the pass, with every lane busy
+// (the decision reads the rectangle, the ranges and the bit; in the pass a warp would run it for a few
+// lanes at a time); once the list is full it is decided on the spot.
+__device__ __noinline__ void sparse_grain_pass(const PixelwiseArgs &a, const PwSparseGrid &g) {
+    PwSparseShared &S = sparse_smem();
+    using C = PwSparse;
+    constexpr int B = PwSparse::kGmBins;
+    PwSparseGrainMajor &M = S.gm;
+    const float z = a.zoom, iz = a.inv_zoom, zr = a.zoom * 1.0000039f;  // (1 + 2^-18): sqrt's rounding
+    const int ng = S.ngrains;
+    for (int t = threadIdx.x; t < ng; t += blockDim.x) {
+        const float4 G = S.grains[t];
+        if (!(G.z >= 0.0f)) continue;  // a radius <= 0 covers nothing
+        const float w = fmaf(sqrtf(G.z), zr, g.gm_eps);  // half-width of the phase band
+        const float px = FG_FSUB(FG_FMUL(G.x, z), 0.5f), py = FG_FSUB(FG_FMUL(G.y, z), 0.5f);
+        float lx = FG_FSUB(FG_FSUB(floorf(px), px), w), ly = FG_FSUB(FG_FSUB(floorf(py), py), w);
+        lx = FG_FSUB(lx, floorf(lx));  // the band starts at phase lx in [0, 1) and spans 2w
+        ly = FG_FSUB(ly, floorf(ly));
+        const int bx0 = min((int)(lx * (float)B), B - 1), bx1 = (int)((lx + 2.0f * w) * (float)B);
+        const int by0 = min((int)(ly * (float)B), B - 1), by1 = (int)((ly + 2.0f * w) * (float)B);
+        const unsigned cell = __float_as_uint(G.w);
+        auto visit = [&](int row, int xb0, int xb1) {  // the entries of bins xb0..xb1 of one bin row
+            const int e1 = M.start[row + xb1 + 1];
+            for (int e = M.start[row + xb0]; e < e1; e++) {
+                const float4 O = M.ent[e];
+                const float rx = gm_pixel(px, O.z), ry = gm_pixel(py, O.w);
+                // xg_of of pixel (rx, ry): rx + 0.5 is exact
+                const float dx = FG_FSUB(FG_FSUB(FG_FMUL(FG_FADD(rx, 0.5f), iz), O.x), G.x);
+                const float dy = FG_FSUB(FG_FSUB(FG_FMUL(FG_FADD(ry, 0.5f), iz), O.y), G.y);
+                if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= G.z) {
+                    const int slot = atomicAdd(&S.nhits, 1);
+                    if (slot < C::kGmHitMax) M.hits[slot] = (unsigned)t | ((unsigned)e << 11);
+                    else sparse_gm_hit(a, S, M.k[e], cell, rx, ry);
+                }
+            }
+        };
+        for (int by = by0; by <= by1; by++) {  // bins past the last wrap to the first
+            const int row = (by & (B - 1)) * B;
+            visit(row, bx0, min(bx1, B - 1));
+            if (bx1 >= B) visit(row, 0, bx1 - B);
+        }
+    }
+    __syncthreads();
+    const int nh = min(S.nhits, C::kGmHitMax);
+    for (int h = threadIdx.x; h < nh; h += blockDim.x) {
+        const unsigned tok = M.hits[h];
+        const int e = (int)(tok >> 11);
+        const float4 G = S.grains[tok & 0x7FFu];
+        const float4 O = M.ent[e];
+        const float rx = gm_pixel(FG_FSUB(FG_FMUL(G.x, z), 0.5f), O.z);
+        const float ry = gm_pixel(FG_FSUB(FG_FMUL(G.y, z), 0.5f), O.w);
+        sparse_gm_hit(a, S, M.k[e], __float_as_uint(G.w), rx, ry);
+    }
+}
+
+// Step 3 in the grain-major form: the owned samples' bit bases (a scan of the rectangles' areas), the
+// phase-binned offsets, then the grains' pass.  Samples whose range leaves the window go to the
+// per-sample loop as in the sample-major form: with every rectangle inside the range table the
+// ownership pass saw them (any_slow); otherwise the plane's ranges span too few cells for any
+// (gm_noslow).
+__device__ __noinline__ void sparse_grain_major(const PixelwiseArgs &a, const PwSparseGrid &g) {
+    PwSparseShared &S = sparse_smem();
+    using C = PwSparse;
+    const int tid = threadIdx.x, nthreads = blockDim.x;
+    PwSparseGrainMajor &M = S.gm;
+    int area = 0;
+    if (tid < a.n) {  // n <= kPwKChunk = the CTA size
+        const int4 R = S.rect[tid];
+        if (R.y > R.x && R.w > R.z) area = (R.y - R.x) * (R.w - R.z);
+    }
+    int total;
+    const int base = block_excl_scan(area, S.wsum, &total);
+    if (tid < a.n) M.base[tid] = base;
+    for (int e = tid; e < a.n; e += nthreads) {
+        M.ent[e] = g.gm_ent[e];
+        M.k[e] = (unsigned short)g.gm_idx[e];
+    }
+    for (int b = tid; b <= C::kGmBins * C::kGmBins; b += nthreads) M.start[b] = (unsigned short)g.gm_idx[a.n + b];
+    for (int w = tid; w < (total + 31) >> 5; w += nthreads) M.bits[w] = 0u;
+    if (tid == 0) S.nhits = 0;
+    __syncthreads();
+    if (!(a.rm > 0.0f)) return;  // a grain radius is at most rm: nothing can cover a sample
+    sparse_grain_pass(a, g);
+    if (S.any_slow) {  // uniform
+        const unsigned slow = sparse_sample_pass<1>(a, S);
+        if (slow) atomicAdd(&a.diag[0], (unsigned long long)slow);
+    }
+}
+
+__device__ __noinline__ void sparse_slow_sample(const PixelwiseArgs &a, float xg, float yg, int x, int y) {
+    PwSparseShared &S = sparse_smem();
     const int i0 = f2i_floor(FG_FDIV(FG_FSUB(xg, a.rm), a.delta));
     const int i1 = f2i_floor(FG_FDIV(FG_FADD(xg, a.rm), a.delta));
     const int j0 = f2i_floor(FG_FDIV(FG_FSUB(yg, a.rm), a.delta));
@@ -302,7 +473,8 @@ __device__ __noinline__ void sparse_slow_sample(const PixelwiseArgs &a, PwSparse
 // Step 2, out of line: the list of non-empty cells (column-major) with the rank before each mask
 // word, then their grain counts, CSR prefix and grains.  Returns false (uniformly) when the list or
 // the grains overflow their shared-memory buffers.
-__device__ __noinline__ bool sparse_stage(const PixelwiseArgs &a, PwSparseShared &S) {
+__device__ __noinline__ bool sparse_stage(const PixelwiseArgs &a) {
+    PwSparseShared &S = sparse_smem();
     using C = PwSparse;
     const int tid = threadIdx.x, nthreads = blockDim.x, lane = tid & 31;
     const int Wc = S.Wc, Hc = S.Hc, hs = S.hs, wi0 = S.wi0, wj0 = S.wj0;
@@ -313,19 +485,19 @@ __device__ __noinline__ bool sparse_stage(const PixelwiseArgs &a, PwSparseShared
         const int per = (nwords + nthreads - 1) / nthreads;
         const int b = tid * per, e = min(nwords, b + per);
         int local = 0;
-        for (int w = b; w < e; w++) local += __popc(S.mask2[w].x);
+        for (int w = b; w < e; w++) local += __popc(S.w.mask2[w].x);
         int total;
         int run = block_excl_scan(local, S.wsum, &total);
         nlist = total;
         if (total <= C::kListMax) {
             for (int w = b; w < e; w++) {
-                S.wrank[w] = (unsigned short)run;
-                unsigned m = S.mask2[w].x;
+                S.w.wrank[w] = (unsigned short)run;
+                unsigned m = S.w.mask2[w].x;
                 const int col = w / hs, row0 = (w - col * hs) * 32;
                 while (m) {
                     const int bit = __ffs(m) - 1;
                     m &= m - 1u;
-                    S.list[run++] = (unsigned short)(col * Hc + row0 + bit);
+                    S.w.list[run++] = (unsigned short)(col * Hc + row0 + bit);
                 }
             }
         }
@@ -343,11 +515,12 @@ __device__ __noinline__ bool sparse_stage(const PixelwiseArgs &a, PwSparseShared
         uint32_t q = 0u;
         Xoshiro rng;
         if (t < nlist) {
-            const int c = S.list[t];
+            const int c = S.w.list[t];
             i = wi0 + c / Hc;
             j = wj0 + c % Hc;
             q = sparse_cell_count(a, i, j, &rng);
         }
+        const float cellw = __uint_as_float((unsigned)(i - wi0) | ((unsigned)(j - wj0) << 16));
         const int qc = (int)min(q, (uint32_t)C::kGrainMax + 1u);
         int incl = qc;
 #pragma unroll
@@ -360,7 +533,7 @@ __device__ __noinline__ bool sparse_stage(const PixelwiseArgs &a, PwSparseShared
         base = __shfl_sync(0xffffffffu, base, 31);
         const int first = base + incl - qc;
         if (t < nlist) {
-            S.gsc[t] = (unsigned)(first & 0xFFFF) | ((unsigned)min(qc, 0xFFFF) << 16);
+            S.w.gsc[t] = (unsigned)(first & 0xFFFF) | ((unsigned)min(qc, 0xFFFF) << 16);
             if (first + qc <= C::kGrainMax) {
                 const float sx = FG_FMUL((float)i, a.delta), sy = FG_FMUL((float)j, a.delta);
                 for (int k = 0; k < qc; k++) {
@@ -369,7 +542,7 @@ __device__ __noinline__ bool sparse_stage(const PixelwiseArgs &a, PwSparseShared
                     float r = radius_draw(a, rng);
                     if (r > a.rm) r = a.rm;
                     const float rr = (r <= 0.0f) ? -1.0f : FG_FMUL(r, r);  // -1 never passes the disk test
-                    S.grains[first + k] = make_float4(cx, cy, rr, 0.0f);
+                    S.grains[first + k] = make_float4(cx, cy, rr, cellw);
                 }
             }
         }
@@ -378,13 +551,13 @@ __device__ __noinline__ bool sparse_stage(const PixelwiseArgs &a, PwSparseShared
     return S.ngrains <= C::kGrainMax;  // an overflow wrote no grain past the buffer; the block is redone
 }
 
-// One block of edge bs at block coordinates (bx, by) (all threads of the CTA; `smem_raw` holds
-// PwSparseShared): 0 rendered (or nothing to render), 1 left undone (its buffers would overflow:
+// One block of edge bs at block coordinates (bx, by) (all threads of the CTA; the dynamic shared memory
+// holds PwSparseShared): 0 rendered (or nothing to render), 1 left undone (its buffers would overflow:
 // nothing written), 2 stopped by cancellation.
 __device__ __noinline__ int pixelwise_sparse_block(const PixelwiseArgs &a, const PwSparseGrid &g, float bs, int bx,
-                                                   int by, unsigned char *smem_raw) {
+                                                   int by) {
     using C = PwSparse;
-    PwSparseShared &S = *reinterpret_cast<PwSparseShared *>(smem_raw);
+    PwSparseShared &S = sparse_smem();
     const int tid = threadIdx.x, nthreads = blockDim.x, lane = tid & 31;
     // the cancellation word, read now and tested after the ownership pass (its latency overlaps it)
     int cancel_seen = 0;
@@ -410,6 +583,7 @@ __device__ __noinline__ int pixelwise_sparse_block(const PixelwiseArgs &a, const
         S.est_cells = 0.0f;
         S.fx0 = 0x7fffffff; S.fx1 = -1; S.fy0 = 0x7fffffff; S.fy1 = -1; S.nsamples = 0;
         S.rw_min = 0x7fffffff; S.rw_max = -1; S.rh_min = 0x7fffffff; S.rh_max = -1;
+        S.any_slow = 0;
     }
     __syncthreads();
     // ---- expected grains and non-empty cells of the window: lambda integrated over its rectangle (a
@@ -447,6 +621,7 @@ __device__ __noinline__ int pixelwise_sparse_block(const PixelwiseArgs &a, const
     {
         int lx0 = 0x7fffffff, lx1 = -1, ly0 = 0x7fffffff, ly1 = -1, ns = 0;
         int wmin = 0x7fffffff, wmax = -1, hmin = 0x7fffffff, hmax = -1;
+        bool slow = false;
         for (int k = tid; k < a.n; k += nthreads) {
             const float2 o = a.offs[k];
             const int xa = first_at_least(X0, a.out_w, a.inv_zoom, a.zoom, o.x);
@@ -455,12 +630,16 @@ __device__ __noinline__ int pixelwise_sparse_block(const PixelwiseArgs &a, const
             const int ye = first_at_least(Y1, a.out_h, a.inv_zoom, a.zoom, o.y);
             S.rect[k] = make_int4(xa, xe, ya, ye);
             // the cell ranges of the rectangle's first columns and rows (pixelwise_sparse_block's table)
-            for (int s2 = 0; s2 < min(xe - xa, C::kRangeSlots); s2++)
-                S.range_x[s2 * a.n + k] =
-                    (unsigned short)sparse_range_code(xg_of(xa + s2, a.inv_zoom, o.x), a.rm, a.delta, wi0, wi1);
-            for (int s2 = 0; s2 < min(ye - ya, C::kRangeSlots); s2++)
-                S.range_y[s2 * a.n + k] =
-                    (unsigned short)sparse_range_code(xg_of(ya + s2, a.inv_zoom, o.y), a.rm, a.delta, wj0, wj1);
+            for (int s2 = 0; s2 < min(xe - xa, C::kRangeSlots); s2++) {
+                const unsigned c = sparse_range_code(xg_of(xa + s2, a.inv_zoom, o.x), a.rm, a.delta, wi0, wi1);
+                S.range_x[s2 * a.n + k] = (unsigned short)c;
+                slow |= c == kRangeSlow;
+            }
+            for (int s2 = 0; s2 < min(ye - ya, C::kRangeSlots); s2++) {
+                const unsigned c = sparse_range_code(xg_of(ya + s2, a.inv_zoom, o.y), a.rm, a.delta, wj0, wj1);
+                S.range_y[s2 * a.n + k] = (unsigned short)c;
+                slow |= c == kRangeSlow;
+            }
             wmin = min(wmin, xe - xa); wmax = max(wmax, xe - xa);
             hmin = min(hmin, ye - ya); hmax = max(hmax, ye - ya);
             if (xe > xa && ye > ya) {
@@ -478,7 +657,9 @@ __device__ __noinline__ int pixelwise_sparse_block(const PixelwiseArgs &a, const
         wmax = __reduce_max_sync(0xffffffffu, wmax);
         hmin = __reduce_min_sync(0xffffffffu, hmin);
         hmax = __reduce_max_sync(0xffffffffu, hmax);
+        slow = __any_sync(0xffffffffu, slow);
         if (lane == 0) {
+            if (slow) S.any_slow = 1;
             if (ns > 0) {
                 atomicAdd(&S.nsamples, ns);
                 atomicMin(&S.fx0, lx0); atomicMax(&S.fx1, lx1);
@@ -518,21 +699,27 @@ __device__ __noinline__ int pixelwise_sparse_block(const PixelwiseArgs &a, const
                 word = __funnelshift_r(lo, hi, rs);
                 if (k == hw - 1) word &= tail;
             }
-            S.mask2[c * hs + k].x = word;
+            S.w.mask2[c * hs + k].x = word;
         }
         __syncthreads();
         for (int w = tid; w < Wc * hs; w += nthreads) {
             const int k = w % hs;
-            S.mask2[w].y = k + 1 < hw ? S.mask2[w + 1].x : 0u;
+            S.w.mask2[w].y = k + 1 < hw ? S.w.mask2[w + 1].x : 0u;
         }
         __syncthreads();
     }
 
     // ---- 2. non-empty cells, their counts and grains
-    if (!sparse_stage(a, S)) return 1;
+    if (!sparse_stage(a)) return 1;
 
-    // ---- 3. the owned samples
-    sparse_samples(a, S);
+    // ---- 3. the owned samples: grain-major when the plane allows it, the samples whose range leaves the
+    // window are known (the plane has none, or every rectangle fits the range table), the samples fit the
+    // bit array and the cost model favours it; else sample-major
+    const bool gm = g.gm_ent && (g.gm_noslow || (S.rw_max <= C::kRangeSlots && S.rh_max <= C::kRangeSlots)) &&
+                    S.nsamples <= 32 * C::kGmBitsWords &&
+                    (float)S.ngrains * g.gm_grain_cost < (float)S.nsamples * g.gm_sample_cost;
+    if (gm) sparse_grain_major(a, g);
+    else sparse_samples(a);
     __syncthreads();
 
     // ---- 4. flush the per-pixel counts
@@ -542,7 +729,10 @@ __device__ __noinline__ int pixelwise_sparse_block(const PixelwiseArgs &a, const
             if (c) atomicAdd(&a.out[(long long)(S.fy0 + t / fw) * a.out_w + (S.fx0 + t % fw)], (float)c);
         }
     }
-    if (tid == 0) atomicAdd(&a.diag[3], 1ull);
+    if (tid == 0) {
+        atomicAdd(&a.diag[3], 1ull);
+        atomicAdd(&a.diag[gm ? 5 : 4], 1ull);
+    }
     return 0;
 }
 
@@ -550,8 +740,8 @@ __device__ __noinline__ int pixelwise_sparse_block(const PixelwiseArgs &a, const
 // a fat-grid block that overflows too is appended to the deferred list for the fat pass (each fat-grid
 // block is either rendered here or listed, never both).
 __device__ __forceinline__ void pixelwise_sparse_root(const PixelwiseArgs &a, const PwSparseGrid &g, int sbx, int sby,
-                                                      int nby, int *list, unsigned char *smem_raw) {
-    const int st = pixelwise_sparse_block(a, g, g.bs, sbx, sby, smem_raw);
+                                                      int nby, int *list) {
+    const int st = pixelwise_sparse_block(a, g, g.bs, sbx, sby);
     if (st != 1) return;
     if (g.ratio == 1) {
         if (threadIdx.x == 0) sparse_defer(a, g, sbx, sby, nby, list);
@@ -561,7 +751,7 @@ __device__ __forceinline__ void pixelwise_sparse_root(const PixelwiseArgs &a, co
         const int bx = sbx * g.ratio + q % g.ratio, by = sby * g.ratio + q / g.ratio;
         if (bx < a.bx0 || bx >= a.bx0 + a.nbx || by < a.by0 || by >= a.by0 + nby) continue;
         __syncthreads();  // the previous block's shared state is no longer read
-        const int sq = pixelwise_sparse_block(a, g, a.bsize, bx, by, smem_raw);
+        const int sq = pixelwise_sparse_block(a, g, a.bsize, bx, by);
         if (sq == 2) return;
         if (sq == 1 && threadIdx.x == 0) list[1 + atomicAdd(list, 1)] = (by - a.by0) * a.nbx + (bx - a.bx0);
     }

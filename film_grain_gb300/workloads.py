@@ -5,7 +5,9 @@ No image dataset is involved: each workload is generated from its seed.
   (the 256 x 256 luma pixel-wise workload).
 - blobs: isotropic Gaussian blobs (amplitude U[0.2, 0.9], sigma U[30, 150] px) over a 0.1 background,
   clamped to [0, 1], each channel seeded independently (the 1024^2 x 3 grain-wise workload and the
-  4096^2 x 3 large-frame workload).
+  4096^2 x 3 large-frame workload).  `scale` shrinks the blobs for small test planes: sixteen blobs of
+  30-150 px on a plane of a few hundred pixels or less add up to a saturated plane, while sigma x
+  max(w, h) / 1536 keeps about half of it near the background and a few percent saturated.
 """
 from __future__ import annotations
 
@@ -19,10 +21,11 @@ def ramp_noise(width: int = 256, height: int = 256, seed: int = 42) -> np.ndarra
     return np.clip(v, 0.0, 1.0).astype(np.float32)
 
 
-def blobs_plane(width: int, height: int, seed: int, n_blobs: int = 16, background: float = 0.1) -> np.ndarray:
+def blobs_plane(width: int, height: int, seed: int, n_blobs: int = 16, background: float = 0.1,
+                scale: float = 1.0) -> np.ndarray:
     rng = np.random.default_rng(seed)
     amp = rng.uniform(0.2, 0.9, n_blobs)
-    sig = rng.uniform(30.0, 150.0, n_blobs)
+    sig = rng.uniform(30.0, 150.0, n_blobs) * scale
     cx = rng.uniform(0, width, n_blobs)
     cy = rng.uniform(0, height, n_blobs)
     xs = np.arange(width, dtype=np.float64) + 0.5
@@ -35,9 +38,14 @@ def blobs_plane(width: int, height: int, seed: int, n_blobs: int = 16, backgroun
     return np.clip(v, 0.0, 1.0).astype(np.float32)
 
 
-def blobs_rgb(width: int, height: int, seed: int) -> np.ndarray:
+def blobs_rgb(width: int, height: int, seed: int, scale: float = 1.0) -> np.ndarray:
     """(H, W, 3) f32 RGB, each channel an independently seeded blob plane."""
-    return np.stack([blobs_plane(width, height, seed * 3 + c) for c in range(3)], axis=-1)
+    return np.stack([blobs_plane(width, height, seed * 3 + c, scale=scale) for c in range(3)], axis=-1)
+
+
+def small_scale(width: int, height: int) -> float:
+    """The blob scale of a small test plane (blobs_plane's `scale`)."""
+    return max(width, height) / 1536.0
 
 
 def gray_rgb(plane: np.ndarray) -> np.ndarray:

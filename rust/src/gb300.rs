@@ -205,6 +205,7 @@ extern "C" {
 
     pub fn fg_last_error_message() -> *const c_char;
     pub fn fg_pixelwise_diagnostics(out: *mut u64);
+    pub fn fg_pixelwise_sparse_forms(out: *mut u64);
     pub fn fg_pixelwise_kernel_count(params: *const FgParams, derived: *const FgDerived, offsets_input: *const f32,
                                      out: *mut i32) -> i32;
     pub fn fg_version() -> *const c_char;

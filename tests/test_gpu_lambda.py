@@ -42,7 +42,7 @@ def test_device_lambda_every_reachable_input(cuda, fgl):
 def test_device_normalize_and_lambda_from_plane(cuda, fgl):
     torch = cuda
     rng = np.random.default_rng(5)
-    planes = [workloads.blobs_plane(320, 200, 2),                                  # already in [0, 1]
+    planes = [workloads.blobs_plane(320, 200, 2, scale=workloads.small_scale(320, 200)),  # already in [0, 1]
               (rng.random((256, 256)) * 3.7).astype(np.float32),                    # normalised by its max
               np.where(rng.random((64, 96)) < 0.01, np.nan, rng.random((64, 96))).astype(np.float32),
               np.full((17, 13), 0.25, np.float32),

@@ -49,7 +49,8 @@ def _check(algo, fgl, orc, plane, **kw):
 
 
 def _blobs(w, h, seed=11):
-    return workloads.blobs_plane(w, h, seed)
+    """A blob plane with blobs scaled to its size: dark background, mid tones and saturated spots."""
+    return workloads.blobs_plane(w, h, seed, scale=workloads.small_scale(w, h))
 
 
 # ------------------------------------------------------------------ pixel-wise
@@ -152,12 +153,31 @@ def test_pixelwise_sparse_pass_forms(cuda, fgl, orc, n, zoom, dist, radius):
     """The sparse block pass (6 launches) in its forms: one offset per thread (N = 256) or several
     threads per offset sharing its rows (N 64, 16); rectangles within the 4 x 4 range table (zoom 1) or
     beyond it (zoom 2: cell ranges computed per sample); zoom 0.5; on a plane large enough for the
-    4 x 4-pixel blocks, mixing dense and sparse regions."""
+    4 x 4-pixel blocks, mixing dense and sparse regions.  The sample step runs grain-major (each staged
+    grain tests the samples within its radius) at N = 256, sample-major where a grain can reach half a
+    pixel (log-normal r 0.15: max radius 0.46)."""
     plane = _blobs(160, 128, seed=5)
     kw = dict(radius=radius, dist=dist, sd=0.4 * radius if dist == "lognorm" else 0.0, zoom=zoom, n=n, seed=41)
     p, d, *_ = _setup(fgl, orc, plane, **kw)
     assert fgl.pixelwise_kernel_count(p, d) == 6
     _check("pixel", fgl, orc, plane, **kw)
+    sample_major, grain_major = fgl.pixelwise_sparse_forms()
+    if n == 256:
+        assert grain_major > 0
+    if radius == 0.15:
+        assert sample_major > 0 and grain_major == 0
+
+
+@pytest.mark.parametrize("radius,n,zoom", [(0.025, 256, 1.0), (0.05, 128, 0.75), (0.1, 64, 1.0), (0.04, 32, 3.0)])
+def test_pixelwise_grain_major_form(cuda, fgl, orc, radius, n, zoom):
+    """The sparse pass's grain-major form against the oracle: log-normal radii, zoom in and out (the
+    phase bands wrap and span several bins), N from 32 to 256, a plane with dense blobs and empty
+    regions."""
+    plane = _blobs(144, 112, seed=9)
+    kw = dict(radius=radius, dist="lognorm", sd=0.4 * radius, zoom=zoom, n=n, seed=77)
+    _check("pixel", fgl, orc, plane, **kw)
+    sample_major, grain_major = fgl.pixelwise_sparse_forms()
+    assert grain_major > 0
 
 
 def test_pixelwise_empty_and_tiny(cuda, fgl, orc):
@@ -211,7 +231,7 @@ def test_grainwise_forced_size(cuda, fgl, orc):
 @pytest.mark.parametrize("mode", ["luma", "rgb"])
 @pytest.mark.parametrize("algo", ["pixel", "grain"])
 def test_render_image_matches_oracle(cuda, fgl, orc, mode, algo):
-    rgb = workloads.blobs_rgb(48, 40, 3)
+    rgb = workloads.blobs_rgb(48, 40, 3, scale=workloads.small_scale(48, 40))
     p = fgl.ParamsBuilder(radius_mean=0.1, n_samples=24, zoom=1.5, seed=77,
                           color_mode=fgl.ColorMode.Luma if mode == "luma" else fgl.ColorMode.Rgb,
                           algo=fgl.Algo.Pixel if algo == "pixel" else fgl.Algo.Grain).build()
@@ -224,7 +244,7 @@ def test_render_image_matches_oracle(cuda, fgl, orc, mode, algo):
 
 
 def test_render_image_roi(cuda, fgl, orc):
-    rgb = workloads.blobs_rgb(64, 64, 4)
+    rgb = workloads.blobs_rgb(64, 64, 4, scale=workloads.small_scale(64, 64))
     p = fgl.ParamsBuilder(radius_mean=0.1, n_samples=16, seed=5, roi=fgl.Roi(8, 4, 40, 36)).build()
     got, stats = fgl.render_with_input_image(rgb, p)
     op = orc.params_struct("const", 0.1, 0.0, 1.0, 0.8, 16, 5)

@@ -30,7 +30,7 @@ def test_noalloc_matches_pixelwise_two_calls(cuda, fgl):
     L = fgl.lib()
     cases = [
         _case(fgl, workloads.ramp_noise(256, 256, 42), radius_mean=0.12, n_samples=64, seed=42),
-        _case(fgl, workloads.blobs_plane(160, 120, 5), radius_mean=0.05, radius_dist=fgl.RadiusDist.Lognorm,
+        _case(fgl, workloads.blobs_plane(160, 120, 5, scale=workloads.small_scale(160, 120)), radius_mean=0.05, radius_dist=fgl.RadiusDist.Lognorm,
               radius_stddev=0.025, zoom=1.5, n_samples=37, seed=9),
     ]
     for p, d, lam in cases:
@@ -78,7 +78,7 @@ def test_noalloc_fills_its_cell_table_exactly(cuda, fgl):
     """A 512 x 512 input plane fills the scratch's cell table to the last entry; N = 4096 fills its
     offset slots.  Both equal the regular render bit for bit."""
     torch = cuda
-    for plane, kw in ((workloads.blobs_plane(512, 512, 11), dict(radius_mean=0.1, n_samples=16, seed=3)),
+    for plane, kw in ((workloads.blobs_plane(512, 512, 11, scale=workloads.small_scale(512, 512)), dict(radius_mean=0.1, n_samples=16, seed=3)),
                       (workloads.ramp_noise(48, 40, 2), dict(radius_mean=0.12, n_samples=4096, seed=5))):
         p, d, lam = _case(fgl, plane, **kw)
         want = fgl.render_pixelwise(lam, p, d)
@@ -105,7 +105,7 @@ from film_grain_gb300 import workloads
 cands = sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*")) + sorted(glob.glob("/usr/local/cuda/targets/*/lib/libcudart.so*"))
 rt = ctypes.CDLL(cands[0])
 L = fg.lib()
-plane = workloads.blobs_plane(96, 80, 4)
+plane = workloads.blobs_plane(96, 80, 4, scale=workloads.small_scale(96, 80))
 p = fg.ParamsBuilder(radius_mean=0.1, n_samples=24, seed=8).build()
 d = fg.derive_common(p, (96, 80))
 lam = fg.lambda_plane(fg.normalize_plane(plane)[0], d.inv_e_pi_r2)
