@@ -334,22 +334,23 @@ __device__ __noinline__ void sparse_samples(const PixelwiseArgs &a) {
 }
 
 // A disk test of the grain-major form passed: grain (window cell `cell`) covers the sample of offset
-// k at pixel (rx, ry).  The sample counts when this block owns it, its cell ranges lie inside the
+// entry e at pixel (rx, ry).  The sample counts when this block owns it, its cell ranges lie inside the
 // window (else pass 1 decides it), the grain's cell lies in its ranges -- the cells the reference
 // visits for it (src/pixelwise.rs:55-58) -- and no other grain covered it before.  The ranges come
 // from the table, or beyond its slots are computed as the table's entries are.
-__device__ __forceinline__ void sparse_gm_hit(const PixelwiseArgs &a, PwSparseShared &S, int k, unsigned cell, float rx,
+__device__ __forceinline__ void sparse_gm_hit(const PixelwiseArgs &a, PwSparseShared &S, int e, unsigned cell, float rx,
                                               float ry) {
     using C = PwSparse;
+    const int k = S.gm.k[e];
     const int x = (int)rx, y = (int)ry;
     const int4 R = S.rect[k];
     if (x < R.x || x >= R.y || y < R.z || y >= R.w) return;  // another block's sample
     const int sx = x - R.x, sy = y - R.z;
-    const float2 o = a.offs[k];
-    const unsigned cx = sx < C::kRangeSlots ? S.range_x[sx * a.n + k]
-                                            : sparse_range_code(xg_of(x, a.inv_zoom, o.x), a.rm, a.delta, S.wi0, S.wi1);
-    const unsigned cy = sy < C::kRangeSlots ? S.range_y[sy * a.n + k]
-                                            : sparse_range_code(xg_of(y, a.inv_zoom, o.y), a.rm, a.delta, S.wj0, S.wj1);
+    unsigned cx, cy;
+    if (sx < C::kRangeSlots) cx = S.range_x[sx * a.n + k];
+    else cx = sparse_range_code(xg_of(x, a.inv_zoom, S.gm.ent[e].x), a.rm, a.delta, S.wi0, S.wi1);
+    if (sy < C::kRangeSlots) cy = S.range_y[sy * a.n + k];
+    else cy = sparse_range_code(xg_of(y, a.inv_zoom, S.gm.ent[e].y), a.rm, a.delta, S.wj0, S.wj1);
     if (cx == kRangeSlow || cy == kRangeSlow) return;
     if ((cell & 0xFFFFu) - (cx & 0x7FFu) > (cx >> 11) || (cell >> 16) - (cy & 0x7FFu) > (cy >> 11)) return;
     const int idx = S.gm.base[k] + sy * (R.y - R.x) + sx;
@@ -372,9 +373,10 @@ __device__ __forceinline__ float gm_pixel(float p, float oz) {
     return FG_FSUB(FG_FADD(FG_FADD(p, oz), kRint), kRint);
 }
 
-// A passed disk test is listed as grain | entry << 11 and decided after the pass, with every lane busy
-// (the decision reads the rectangle, the ranges and the bit; in the pass a warp would run it for a few
-// lanes at a time); once the list is full it is decided on the spot.
+// A passed disk test is listed as grain | entry << 11 and decided after the pass, the list dealt across
+// all lanes (the decision reads the rectangle, the ranges and the bit; in the pass a warp would run it
+// for a few lanes at a time, and a lane deciding its own tests leaves the warp as slow as its busiest
+// lane: both measured slower); once the list is full a test is decided on the spot.
 __device__ __noinline__ void sparse_grain_pass(const PixelwiseArgs &a, const PwSparseGrid &g) {
     PwSparseShared &S = sparse_smem();
     using C = PwSparse;
@@ -404,7 +406,7 @@ __device__ __noinline__ void sparse_grain_pass(const PixelwiseArgs &a, const PwS
                 if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= G.z) {
                     const int slot = atomicAdd(&S.nhits, 1);
                     if (slot < C::kGmHitMax) M.hits[slot] = (unsigned)t | ((unsigned)e << 11);
-                    else sparse_gm_hit(a, S, M.k[e], cell, rx, ry);
+                    else sparse_gm_hit(a, S, e, cell, rx, ry);
                 }
             }
         };
@@ -423,7 +425,7 @@ __device__ __noinline__ void sparse_grain_pass(const PixelwiseArgs &a, const PwS
         const float4 O = M.ent[e];
         const float rx = gm_pixel(FG_FSUB(FG_FMUL(G.x, z), 0.5f), O.z);
         const float ry = gm_pixel(FG_FSUB(FG_FMUL(G.y, z), 0.5f), O.w);
-        sparse_gm_hit(a, S, M.k[e], __float_as_uint(G.w), rx, ry);
+        sparse_gm_hit(a, S, e, __float_as_uint(G.w), rx, ry);
     }
 }
 
