@@ -41,7 +41,8 @@ struct PwSparse {
     static constexpr int kRangeSlots = 4;    // tabulated cell ranges per offset and axis
     static constexpr int kGmBins = 16;       // phase bins per axis of the grain-major form's offset table
     static constexpr int kGmBitsWords = 1024;  // owned-sample bits of the grain-major form
-    static constexpr int kGmHitMax = 3584;     // disk tests passed, listed for the hits' pass
+    static constexpr int kGmHitMax = 2560;     // disk tests passed, listed for the hits' pass
+    static constexpr int kGmPairs = 256;       // a warp's queue of (grain, entry) candidates
 };
 
 // Mask words per window column in shared memory: the column's words rounded up to an odd count, so
@@ -74,6 +75,7 @@ struct PwSparseGrainMajor {
     int base[kPwKChunk];                         // first bit of each offset's owned samples
     unsigned int bits[PwSparse::kGmBitsWords];   // one per owned sample: covered by a grain already
     unsigned int hits[PwSparse::kGmHitMax];      // (grain, entry) pairs that passed the disk test
+    unsigned short pairs[(PwSparse::kThreads / 32) * PwSparse::kGmPairs];  // per warp: lane << 8 | entry
 };
 
 struct PwSparseShared {
@@ -99,6 +101,7 @@ struct PwSparseShared {
 
 static_assert(sizeof(PwSparseGrainMajor) <= sizeof(PwSparseWindow), "the grain-major tables fit the window's space");
 static_assert(PwSparse::kGrainMax <= 2048, "a listed hit holds the grain in 11 bits");
+static_assert(kPwKChunk <= 256, "a queued candidate holds the entry in 8 bits");
 
 // The CTA's PwSparseShared: the start of its dynamic shared memory, named through the shared array
 // itself, so that the out-of-line functions below address it as shared memory (a reference passed in
@@ -377,43 +380,84 @@ __device__ __forceinline__ float gm_pixel(float p, float oz) {
 // all lanes (the decision reads the rectangle, the ranges and the bit; in the pass a warp would run it
 // for a few lanes at a time, and a lane deciding its own tests leaves the warp as slow as its busiest
 // lane: both measured slower); once the list is full a test is decided on the spot.
+__device__ __forceinline__ void gm_pass_test(const PixelwiseArgs &a, PwSparseShared &S, int t, int e) {
+    using C = PwSparse;
+    const float4 G = S.grains[t];
+    const float4 O = S.gm.ent[e];
+    const float px = FG_FSUB(FG_FMUL(G.x, a.zoom), 0.5f), py = FG_FSUB(FG_FMUL(G.y, a.zoom), 0.5f);
+    const float rx = gm_pixel(px, O.z), ry = gm_pixel(py, O.w);
+    // xg_of of pixel (rx, ry): rx + 0.5 is exact
+    const float dx = FG_FSUB(FG_FSUB(FG_FMUL(FG_FADD(rx, 0.5f), a.inv_zoom), O.x), G.x);
+    const float dy = FG_FSUB(FG_FSUB(FG_FMUL(FG_FADD(ry, 0.5f), a.inv_zoom), O.y), G.y);
+    if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= G.z) {
+        const int slot = atomicAdd(&S.nhits, 1);
+        if (slot < C::kGmHitMax) S.gm.hits[slot] = (unsigned)t | ((unsigned)e << 11);
+        else sparse_gm_hit(a, S, e, __float_as_uint(G.w), rx, ry);
+    }
+}
+
+// A warp takes 32 grains at a time, one per lane: each lane finds its grain's band of bins and counts
+// the entries in them (3.5 on the large frame, 0 to 8 typically), the warp lists its (grain, entry)
+// candidates in its queue at the lanes' prefix of the counts, and then tests the listed candidates 32
+// at a time, every lane busy (a lane testing its own grain's candidates leaves the warp waiting for its
+// busiest lane); a round with more candidates than the queue holds is tested lane by lane.
 __device__ __noinline__ void sparse_grain_pass(const PixelwiseArgs &a, const PwSparseGrid &g) {
     PwSparseShared &S = sparse_smem();
     using C = PwSparse;
     constexpr int B = PwSparse::kGmBins;
     PwSparseGrainMajor &M = S.gm;
-    const float z = a.zoom, iz = a.inv_zoom, zr = a.zoom * 1.0000039f;  // (1 + 2^-18): sqrt's rounding
-    const int ng = S.ngrains;
-    for (int t = threadIdx.x; t < ng; t += blockDim.x) {
-        const float4 G = S.grains[t];
-        if (!(G.z >= 0.0f)) continue;  // a radius <= 0 covers nothing
-        const float w = fmaf(sqrtf(G.z), zr, g.gm_eps);  // half-width of the phase band
-        const float px = FG_FSUB(FG_FMUL(G.x, z), 0.5f), py = FG_FSUB(FG_FMUL(G.y, z), 0.5f);
-        float lx = FG_FSUB(FG_FSUB(floorf(px), px), w), ly = FG_FSUB(FG_FSUB(floorf(py), py), w);
-        lx = FG_FSUB(lx, floorf(lx));  // the band starts at phase lx in [0, 1) and spans 2w
-        ly = FG_FSUB(ly, floorf(ly));
-        const int bx0 = min((int)(lx * (float)B), B - 1), bx1 = (int)((lx + 2.0f * w) * (float)B);
-        const int by0 = min((int)(ly * (float)B), B - 1), by1 = (int)((ly + 2.0f * w) * (float)B);
-        const unsigned cell = __float_as_uint(G.w);
-        auto visit = [&](int row, int xb0, int xb1) {  // the entries of bins xb0..xb1 of one bin row
-            const int e1 = M.start[row + xb1 + 1];
-            for (int e = M.start[row + xb0]; e < e1; e++) {
-                const float4 O = M.ent[e];
-                const float rx = gm_pixel(px, O.z), ry = gm_pixel(py, O.w);
-                // xg_of of pixel (rx, ry): rx + 0.5 is exact
-                const float dx = FG_FSUB(FG_FSUB(FG_FMUL(FG_FADD(rx, 0.5f), iz), O.x), G.x);
-                const float dy = FG_FSUB(FG_FSUB(FG_FMUL(FG_FADD(ry, 0.5f), iz), O.y), G.y);
-                if (FG_FADD(FG_FMUL(dx, dx), FG_FMUL(dy, dy)) <= G.z) {
-                    const int slot = atomicAdd(&S.nhits, 1);
-                    if (slot < C::kGmHitMax) M.hits[slot] = (unsigned)t | ((unsigned)e << 11);
-                    else sparse_gm_hit(a, S, e, cell, rx, ry);
-                }
+    const float z = a.zoom, zr = a.zoom * 1.0000039f;  // (1 + 2^-18): sqrt's rounding
+    const int ng = S.ngrains, lane = threadIdx.x & 31;
+    unsigned short *Q = M.pairs + (threadIdx.x >> 5) * C::kGmPairs;
+    for (int t0 = threadIdx.x & ~31; t0 < ng; t0 += blockDim.x) {  // warp-uniform bounds (the shuffles)
+        const int t = t0 + lane;
+        int bx0 = 0, bx1 = -1, by0 = 0, by1 = -1;  // an empty band unless the grain can cover a sample
+        if (t < ng) {
+            const float4 G = S.grains[t];
+            if (G.z >= 0.0f) {  // a radius <= 0 (r^2 = -1) covers nothing
+                const float w = fmaf(sqrtf(G.z), zr, g.gm_eps);  // half-width of the phase band
+                const float px = FG_FSUB(FG_FMUL(G.x, z), 0.5f), py = FG_FSUB(FG_FMUL(G.y, z), 0.5f);
+                float lx = FG_FSUB(FG_FSUB(floorf(px), px), w), ly = FG_FSUB(FG_FSUB(floorf(py), py), w);
+                lx = FG_FSUB(lx, floorf(lx));  // the band starts at phase lx in [0, 1) and spans 2w
+                ly = FG_FSUB(ly, floorf(ly));
+                bx0 = min((int)(lx * (float)B), B - 1);
+                bx1 = (int)((lx + 2.0f * w) * (float)B);
+                by0 = min((int)(ly * (float)B), B - 1);
+                by1 = (int)((ly + 2.0f * w) * (float)B);
+            }
+        }
+        // the band's entries: bins bx0..bx1 of bin rows by0..by1, bins past the last wrapping to the first
+        auto for_each_range = [&](auto f) {
+            for (int by = by0; by <= by1; by++) {
+                const int row = (by & (B - 1)) * B;
+                f(M.start[row + bx0], M.start[row + min(bx1, B - 1) + 1]);
+                if (bx1 >= B) f(M.start[row], M.start[row + bx1 - B + 1]);
             }
         };
-        for (int by = by0; by <= by1; by++) {  // bins past the last wrap to the first
-            const int row = (by & (B - 1)) * B;
-            visit(row, bx0, min(bx1, B - 1));
-            if (bx1 >= B) visit(row, 0, bx1 - B);
+        int cnt = 0;
+        for_each_range([&](int e0, int e1) { cnt += e1 - e0; });
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (total <= C::kGmPairs) {
+            int q = incl - cnt;
+            for_each_range([&](int e0, int e1) {
+                for (int e = e0; e < e1; e++) Q[q++] = (unsigned short)((lane << 8) | e);
+            });
+            __syncwarp();
+            for (int i = lane; i < total; i += 32) {
+                const unsigned pr = Q[i];
+                gm_pass_test(a, S, t0 + (int)(pr >> 8), (int)(pr & 0xFFu));
+            }
+            __syncwarp();  // the queue is read before the next round writes it
+        } else {
+            for_each_range([&](int e0, int e1) {
+                for (int e = e0; e < e1; e++) gm_pass_test(a, S, t, e);
+            });
         }
     }
     __syncthreads();
