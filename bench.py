@@ -205,11 +205,11 @@ def cpu_pixel_baseline(oracle, planes, wl, threads, rows=None):
 # surrogate input, 373.9 MB read+write for 3 x 1024^2 px; grainwise_persistent_kernel on a 512^2 ->
 # 1024^2 plane of the grain-wise blob frame, 18.25 MB per 1024^2 output pixels (the lambda plane plus the
 # sample-mask lines that miss L2); cell_mask_kernel + pixelwise_sparse_kernel on the 1024^2 flat plane
-# of the large frame's parameters, 170.3 + 250.0 MB per 1024^2 output pixels (the emptiness bitmask
+# of the large frame's parameters, 170.3 + 247.6 MB per 1024^2 output pixels (the emptiness bitmask
 # written, then read with the cell table).
 SG_CONV_DRAM_BYTES_PER_PX = 373.9e6 / (3 * 1024 * 1024)
 GRAINWISE_DRAM_BYTES_PER_OUT_PX = 18.25e6 / (1024 * 1024)
-PIXELWISE_DRAM_BYTES_PER_OUT_PX = (170.3e6 + 250.0e6) / (1024 * 1024)
+PIXELWISE_DRAM_BYTES_PER_OUT_PX = (170.3e6 + 247.6e6) / (1024 * 1024)
 
 # Algorithmic lane-ops of the pixel-wise path (an exact method that hashes every cell once): per cell
 # its hash and first uniform (~65: the row stage of mix3, one SplitMix64, ~24; the four PCG32 seed words
