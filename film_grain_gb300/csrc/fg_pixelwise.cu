@@ -231,10 +231,11 @@ size_t pixelwise_cellmask_bytes(const PixelwiseArgs &a, int nby) {
 // rm * zoom output pixels; the candidate pixel of an offset is exact while that reach plus the f32
 // rounding of the pixel coordinates (eps: a few ulps of the largest coordinate) stays below half a
 // pixel, and the rounding to an integer by adding 1.5 * 2^23 needs coordinates below 2^22.  Costs, in
-// units fitted to timings of both forms (4096^2 planes at r 0.025 log-normal N 256, where grain-major
-// is 20 % faster, and the 256^2 ramp at r 0.12 N 64, where it is 20 % slower): a grain pays its
-// set-up and, per candidate, a disk test and its share of the listed hits, for n (2 (r_mean zoom +
-// eps) + 1/bins)^2 candidates on average; a sample pays the scan of its cell range's columns.
+// units fitted to timings of both forms (on the 4096^2 planes at r 0.025 log-normal N 256 grain-major
+// is faster for every block; on the 256^2 ramp at r 0.12 N 64 it is slower for the dense blocks): a
+// grain pays its set-up and, per candidate, a disk test and its share of the listed hits, for
+// n (2 (r_mean zoom + eps) + 1/bins)^2 candidates on average; a sample pays the scan of its cell
+// range's columns.
 static bool plan_grain_major(const PixelwiseArgs &a, PwSparseGrid *g) {
     const double ext = std::max({std::fabs(a.offx_min), std::fabs(a.offx_max), std::fabs(a.offy_min),
                                  std::fabs(a.offy_max)});
@@ -249,7 +250,7 @@ static bool plan_grain_major(const PixelwiseArgs &a, PwSparseGrid *g) {
     const double span = 2.0 * a.rm / a.delta + 1.0 + 8.0 * grid * 0x1p-23 / a.delta;
     g->gm_noslow = span <= 30.0 ? 1 : 0;
     const double band = 2.0 * ((double)a.radius_mean * a.zoom + eps) + 1.0 / PwSparse::kGmBins;
-    g->gm_grain_cost = (float)(120.0 + 60.0 * a.n * band * band);
+    g->gm_grain_cost = (float)(60.0 + 40.0 * a.n * band * band);
     g->gm_sample_cost = (float)(40.0 + 9.0 * (2.0 * a.rm / a.delta + 1.0));
     return true;
 }
