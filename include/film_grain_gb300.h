@@ -328,17 +328,17 @@ FG_API const char *fg_last_error_message(void);
  * per-sample regeneration path, [1] blocks without a staged cell window, [2] block subdivisions on
  * shared-memory overflow, [3] blocks processed.  No counterpart in the crate (diagnostics only). */
 FG_API void fg_pixelwise_diagnostics(unsigned long long out[4]);
-/* Blocks of the calling thread's last synchronous fg_render_pixelwise that the
- * sparse block pass ran, by the form of their sample step: [0] sample-major (each sample scans the cells
- * of its range), [1] grain-major (each staged grain tests the samples within its radius).  The two forms
- * give identical counts.  No counterpart in the crate (diagnostics only). */
+/* Blocks of the calling thread's last synchronous fg_render_pixelwise that the sparse block pass ran,
+ * by the form of their sample step: [0] sample-major (each sample scans the cells of its range),
+ * [1] grain-major (each staged grain tests the samples within its radius).  The two forms give
+ * identical counts.  No counterpart in the crate (diagnostics only). */
 FG_API void fg_pixelwise_sparse_forms(unsigned long long out[2]);
 /* Kernel launches one pixel-wise render of these params makes: 3 when the plane takes the per-sample
  * kernel (cell table, per-sample kernel, epilogue), 6 when it takes the sparse block pass (cell table,
- * the plane's cell-emptiness bitmask, the offsets sorted by x, sparse and fat block passes, epilogue),
- * 4 when it takes the
- * lean block pass (cell table, lean and fat block passes, epilogue).  offsets_input as for
- * fg_render_pixelwise.  No counterpart in the crate (diagnostics only). */
+ * the plane's cell-emptiness bitmask, the offsets sorted by x and binned by phase, sparse and fat block
+ * passes, epilogue), 4 when it takes the lean block pass (cell table, lean and fat block passes,
+ * epilogue).  offsets_input as for fg_render_pixelwise.  No counterpart in the crate (diagnostics
+ * only). */
 FG_API fg_status fg_pixelwise_kernel_count(const fg_params *params, const fg_derived *derived,
                                            const float *offsets_input, int32_t *out);
 
