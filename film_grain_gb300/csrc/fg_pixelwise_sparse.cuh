@@ -21,9 +21,9 @@
 //      their grains -- contiguous in the CSR, since cells of one column follow each other in the list
 //      -- get the disk test dx*dx + dy*dy <= r*r (src/pixelwise.rs:96-99);
 //      or grain-major (sparse_grain_pass), when a grain's reach is below half an output pixel and the
-//      cost model favours it: each thread takes staged grains, finds the few owned samples within a
-//      grain's radius through a table of the offsets binned by their phase, gives them the same disk
-//      test, and sets a bit per covered sample whose range holds the grain's cell;
+//      cost model favours it: a warp takes 32 staged grains, lists the candidate samples within their
+//      radii through a table of the offsets binned by their phase, gives the candidates the same disk
+//      test 32 at a time, and sets a bit per covered sample whose range holds the grain's cell;
 //   4. hit counts go to per-pixel shared counters, then to the output plane (integers, exact in f32).
 // The indicator is an OR over the grains of the sample's cells, so the result equals the reference's
 // early-exit loop bit for bit.
